@@ -1,0 +1,116 @@
+/*
+ * spock_gb300 -- C ABI of the GB300-native SPOCK solver (risk-averse optimal control on
+ * scenario trees, SuperMann-accelerated Chambolle-Pock).
+ *
+ * Every entry point takes plain pointers and sizes and returns 0 on success or a nonzero
+ * SPOCK_E_* code; spock_last_error() then returns the message (thread-local).  The C++
+ * wrapper include/spock_gb300.hpp rebuilds the reference's class interface on top of this.
+ *
+ * Each declaration names the reference interface it replaces (ruairimoran/spock.cu).
+ */
+#ifndef SPOCK_GB300_H
+#define SPOCK_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPOCK_OK 0
+#define SPOCK_E_INVALID 1  /* invalid argument / malformed data folder (std::invalid_argument) */
+#define SPOCK_E_CUDA 2     /* CUDA runtime failure */
+#define SPOCK_E_UNKNOWN 3
+
+/* Exit statuses of a solve (src/cache.cuh:68-73), plus 3 = stopped on a non-finite residual. */
+#define SPOCK_NOT_RUN (-1)
+#define SPOCK_CONVERGED 0
+#define SPOCK_OUT_OF_ITER 1
+#define SPOCK_OUT_OF_TIME 2
+#define SPOCK_DIVERGED 3
+
+#define SPOCK_ALGO_SPOCK 0 /* Cache::runSpock (src/cache.cuh:1008-1132) */
+#define SPOCK_ALGO_CP 1    /* Cache::runCp    (src/cache.cuh:967-1002) */
+
+typedef struct spock_problem_s *spock_problem; /* ScenarioTree<T> + ProblemData<T> */
+typedef struct spock_solver_s *spock_solver;   /* Cache<T> (one or a batch of instances) */
+
+/* Solver options: the CacheBuilder setters (src/cache.cuh:1154-1210). */
+typedef struct {
+    double tol_abs;        /* toleranceAbsolute (default 1e-3) */
+    double tol_rel;        /* toleranceRelative (default 0) */
+    double max_time_secs;  /* maxTimeSecs (0 = none) */
+    long max_iters;        /* maxIters, outer iterations (0 = unlimited) */
+    long max_inner;        /* maxItersInner (default 8) */
+    long anderson;         /* andersonBuffer (default 3, at most 8) */
+    int precision;         /* 64 (double, the reference's T=double) or 32 (float) */
+    long batch;            /* number of instances solved together (>= 1) */
+    int device;            /* CUDA device ordinal */
+} spock_options;
+
+/* Fills the CacheBuilder defaults (src/cache.cuh:1154-1163): tol_abs 1e-3, tol_rel 0,
+ * max_inner 8, anderson 3; precision 64, batch 1, device 0. */
+void spock_options_default(spock_options *opts);
+
+/* Message of the last failing call on this thread (the reference's static `err` stream,
+ * include/gpu.cuh:24-25, without its accumulation). */
+const char *spock_last_error(void);
+
+/* Load a data folder written by the offline factory: ScenarioTree<T>(path)
+ * (src/tree.cuh:102-179) + ProblemData<T>(tree) (src/problem.cuh:126-153).  Host-side only;
+ * device copies are made per solver. */
+int spock_problem_load(const char *path, spock_problem *out);
+void spock_problem_free(spock_problem p);
+/* sizes[10] = numEvents, numNodes, numNonleafNodes, numStages, numStates, numInputs,
+ * sizePrimal, sizeDual, preconditioned, nullDim  (tree.cuh:207-229, cache.cuh:367-369) */
+int spock_problem_sizes(spock_problem p, long *sizes10);
+/* stepSize (problem.cuh:521) and the preconditioning scaling (nx+nu, ones if none). */
+int spock_problem_step(spock_problem p, double *step, double *scaling_or_null);
+
+/* CacheBuilder<T>(tree, data)...build() (src/cache.cuh:1215-1244). */
+int spock_solver_create(spock_problem p, const spock_options *opts, spock_solver *out);
+void spock_solver_free(spock_solver s);
+
+/* Cache::runSpock / runCp (src/cache.cuh:967-1132) for every instance of the batch.
+ * x0: count*nx host doubles (unscaled, as the user passes them); instance b uses row
+ * b % count.  warm: NULL for a cold start (the reference's reset() + run), else count*(sizePrimal
+ * + sizeDual) previous iterates (the `previousSolution` argument).  statuses/iters: batch
+ * entries each, may be NULL.  Blocks until every instance has stopped. */
+int spock_solve(spock_solver s, int algo, const double *x0, long count, const double *warm, int *statuses, long *iters);
+/* Same, with x0 already on the device as nx x batch values of the solver precision laid out
+ * element-major (x0[c * batch + b]); results stay on the device until read. */
+int spock_solve_device(spock_solver s, int algo, const void *x0_device, int *statuses, long *iters);
+
+/* Results.  Cache::solution() (cache.cuh:378): the raw iterate of one instance, sizePrimal +
+ * sizeDual doubles.  Cache::states()/inputs() (cache.cuh:386-412): unscaled, nx*numNodes and
+ * nu*numNonleafNodes doubles.  first_inputs: the unscaled u_0 of every instance (batch*nu). */
+int spock_get_iterate(spock_solver s, long instance, double *out);
+int spock_get_iterates(spock_solver s, double *out_batch_by_size);
+int spock_get_states_inputs(spock_solver s, long instance, double *states, double *inputs);
+int spock_get_first_inputs(spock_solver s, double *out);
+/* status(), solveIter(), solveTime() (cache.cuh:357-361) of one instance. */
+int spock_status(spock_solver s, long instance, int *status, long *iters, double *seconds);
+/* K0/K1/K2/backtracks/K3 counts, T evaluations and iterations of instance 0 (the debug
+ * counters of cache.cuh:1101-1130). */
+int spock_counters(spock_solver s, long *out7);
+/* reset() (cache.cuh:436-479): zero the iterate. */
+int spock_reset(spock_solver s);
+
+/* Operator-level entry points (the reference tests reach these through friend access,
+ * tests/cuda/testOperator.cu, testCache.cu): single instance, host buffers. */
+int spock_op(spock_solver s, const double *prim, double *dual);            /* LinearOperator::op  (operator.cuh:40-60) */
+int spock_adj(spock_solver s, const double *dual, double *prim);           /* LinearOperator::adj (operator.cuh:62-82) */
+int spock_cp_step(spock_solver s, const double *x0, const double *z, double *cand); /* Cache::iter (cache.cuh:795-801) */
+int spock_apply_m(spock_solver s, const double *z, double *mz);            /* M of Cache::dotM (cache.cuh:721-734) */
+
+/* Measurement hooks for the benchmark: CUDA-event time of one launch of a named kernel
+ * ("lstar", "lop", "mlstar", "mlop", "dyn", "reduce", "update", "teval", "round"), its
+ * algorithmic bytes, and the device time of `rounds` replays of the captured SuperMann round. */
+int spock_kernel_time(spock_solver s, const char *which, int reps, double *ms, long *bytes);
+int spock_round_time(spock_solver s, int rounds, double *ms);
+/* Rounds (one T evaluation + one M application per instance each) and kernel launches of the
+ * last solve. */
+int spock_run_stats(spock_solver s, long *rounds, long *launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,55 @@
+"""Build libspock_gb300.so (CUDA for sm_103a + C++ host + C ABI) in-tree with nvcc.
+
+Usage: python spock.cu_gb300/build.py      (or `build()` from Python)
+Output: spock.cu_gb300/_build/libspock_gb300.so
+"""
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT, "libspock_gb300.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+SOURCES = ["engine.cu", "problem.cpp", "capi.cpp"]
+
+
+def nvcc():
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _compile(src):
+    obj = os.path.join(OUT, os.path.basename(src) + ".o")
+    cmd = [nvcc(), "-c", os.path.join(SRC, src), "-o", obj, "-std=c++17", "-O3", "-lineinfo",
+           "-Xcompiler", "-fPIC,-O3", "--expt-relaxed-constexpr"] + ARCH
+    if src.endswith(".cpp"):
+        cmd[1:1] = ["-x", "cu"]
+    subprocess.check_call(cmd)
+    return obj
+
+
+def build(verbose=False):
+    os.makedirs(OUT, exist_ok=True)
+    srcs = [os.path.join(SRC, s) for s in SOURCES]
+    hdrs = [os.path.join(SRC, f) for f in os.listdir(SRC) if f.endswith((".cuh", ".hpp", ".h"))]
+    hdrs.append(os.path.join(HERE, "..", "include", "spock_gb300.h"))
+    if os.path.exists(LIB):
+        newest = max(os.path.getmtime(f) for f in srcs + hdrs)
+        if os.path.getmtime(LIB) >= newest:
+            return LIB
+    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+        objs = list(ex.map(_compile, SOURCES))
+    subprocess.check_call([nvcc(), "-shared", "-o", LIB + ".tmp"] + objs + ARCH + ["-lcudart"])
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose=True))
+    sys.exit(0)

@@ -1,0 +1,291 @@
+// C ABI (include/spock_gb300.h) over the engine.  Exceptions never cross the boundary:
+// they become SPOCK_E_* codes with the message kept for spock_last_error().
+#include "../../include/spock_gb300.h"
+
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+
+#include "engine.cuh"
+#include "problem.hpp"
+
+struct spock_problem_s {
+    spock::HostProblem hp;
+};
+
+struct spock_solver_s {
+    std::unique_ptr<spock::EngineBase> eng;
+    std::vector<int> status;
+    std::vector<long> iters;
+    double seconds = 0;
+};
+
+namespace {
+thread_local std::string g_error;
+
+template <typename F>
+int guard(F &&f) {
+    try {
+        f();
+        return SPOCK_OK;
+    } catch (const std::invalid_argument &e) {
+        g_error = e.what();
+        return SPOCK_E_INVALID;
+    } catch (const std::runtime_error &e) {
+        g_error = e.what();
+        return SPOCK_E_CUDA;
+    } catch (const std::exception &e) {
+        g_error = e.what();
+        return SPOCK_E_UNKNOWN;
+    } catch (...) {
+        g_error = "unknown error";
+        return SPOCK_E_UNKNOWN;
+    }
+}
+
+void need(const void *p, const char *what) {
+    if (!p) throw std::invalid_argument(std::string("[spock] null argument: ") + what);
+}
+
+spock_solver_s *solver(spock_solver s) {
+    need(s, "solver");
+    return s;
+}
+}  // namespace
+
+extern "C" {
+
+void spock_options_default(spock_options *o) {
+    if (!o) return;
+    o->tol_abs = 1e-3;
+    o->tol_rel = 0.;
+    o->max_time_secs = 0.;
+    o->max_iters = 0;
+    o->max_inner = 8;
+    o->anderson = 3;
+    o->precision = 64;
+    o->batch = 1;
+    o->device = 0;
+}
+
+const char *spock_last_error(void) { return g_error.c_str(); }
+
+int spock_problem_load(const char *path, spock_problem *out) {
+    return guard([&] {
+        need(path, "path");
+        need(out, "out");
+        auto p = std::make_unique<spock_problem_s>();
+        p->hp = spock::HostProblem::load(path);
+        *out = p.release();
+    });
+}
+
+void spock_problem_free(spock_problem p) { delete p; }
+
+int spock_problem_sizes(spock_problem p, long *s) {
+    return guard([&] {
+        need(p, "problem");
+        need(s, "sizes");
+        const auto &h = p->hp;
+        long v[10] = {h.numEvents, h.numNodes, h.numNonleaf, h.numStages, h.nx, h.nu, h.sizePrim, h.sizeDual,
+                      h.preconditioned ? 1L : 0L, h.nullDim};
+        std::memcpy(s, v, sizeof v);
+    });
+}
+
+int spock_problem_step(spock_problem p, double *step, double *scaling) {
+    return guard([&] {
+        need(p, "problem");
+        if (step) *step = p->hp.stepSize;
+        if (scaling) std::memcpy(scaling, p->hp.scaling.data(), sizeof(double) * p->hp.scaling.size());
+    });
+}
+
+int spock_solver_create(spock_problem p, const spock_options *o, spock_solver *out) {
+    return guard([&] {
+        need(p, "problem");
+        need(out, "out");
+        spock_options def;
+        spock_options_default(&def);
+        if (!o) o = &def;
+        if (o->tol_abs < 0 || o->tol_rel < 0 || o->max_time_secs < 0 || o->max_iters < 0 || o->max_inner < 1)
+            throw std::invalid_argument("[CacheBuilder] negative tolerance/time/iterations");
+        spock::Options opt;
+        opt.tolAbs = o->tol_abs;
+        opt.tolRel = o->tol_rel;
+        opt.maxTimeSecs = o->max_time_secs;
+        opt.maxOuter = o->max_iters;
+        opt.maxInner = o->max_inner;
+        opt.anderson = o->anderson;
+        auto s = std::make_unique<spock_solver_s>();
+        s->eng.reset(spock::makeEngine(p->hp, opt, o->batch, o->precision, o->device));
+        s->status.assign(o->batch, SPOCK_NOT_RUN);
+        s->iters.assign(o->batch, 0);
+        *out = s.release();
+    });
+}
+
+void spock_solver_free(spock_solver s) { delete s; }
+
+static void finishSolve(spock_solver_s *s, int *statuses, long *iters) {
+    s->eng->getStatus(s->status.data(), s->iters.data());
+    s->seconds = s->eng->lastSeconds();
+    const long B = s->eng->batch();
+    for (long b = 0; b < B; b++) {
+        if (statuses) statuses[b] = s->status[b];
+        if (iters) iters[b] = s->iters[b];
+    }
+}
+
+int spock_solve(spock_solver sv, int algo, const double *x0, long count, const double *warm, int *statuses, long *iters) {
+    return guard([&] {
+        auto *s = solver(sv);
+        need(x0, "x0");
+        if (algo != SPOCK_ALGO_SPOCK && algo != SPOCK_ALGO_CP) throw std::invalid_argument("[Cache] unknown algorithm");
+        s->eng->setInitialStates(x0, count);
+        if (warm) s->eng->setIterate(warm, count);
+        s->eng->run(algo == SPOCK_ALGO_SPOCK ? spock::kSpock : spock::kCp, warm != nullptr);
+        finishSolve(s, statuses, iters);
+    });
+}
+
+int spock_solve_device(spock_solver sv, int algo, const void *x0, int *statuses, long *iters) {
+    return guard([&] {
+        auto *s = solver(sv);
+        need(x0, "x0");
+        s->eng->setInitialStatesDevice(x0, s->eng->batch());
+        s->eng->run(algo == SPOCK_ALGO_SPOCK ? spock::kSpock : spock::kCp, false);
+        finishSolve(s, statuses, iters);
+    });
+}
+
+int spock_get_iterate(spock_solver sv, long instance, double *out) {
+    return guard([&] {
+        auto *s = solver(sv);
+        need(out, "out");
+        s->eng->getIterate(instance, out);
+    });
+}
+
+int spock_get_iterates(spock_solver sv, double *out) {
+    return guard([&] {
+        auto *s = solver(sv);
+        need(out, "out");
+        s->eng->getIterates(out);
+    });
+}
+
+int spock_get_states_inputs(spock_solver sv, long instance, double *states, double *inputs) {
+    return guard([&] {
+        auto *s = solver(sv);
+        const auto &h = s->eng->problem();
+        std::vector<double> z(h.sizeIterate());
+        s->eng->getIterate(instance, z.data());
+        if (states)
+            for (long j = 0; j < h.numNodes; j++)
+                for (long k = 0; k < h.nx; k++) states[j * h.nx + k] = z[h.sizeU + j * h.nx + k] / h.scaling[k];
+        if (inputs)
+            for (long i = 0; i < h.numNonleaf; i++)
+                for (long k = 0; k < h.nu; k++) inputs[i * h.nu + k] = z[i * h.nu + k] / h.scaling[h.nx + k];
+    });
+}
+
+int spock_get_first_inputs(spock_solver sv, double *out) {
+    return guard([&] {
+        auto *s = solver(sv);
+        need(out, "out");
+        s->eng->getFirstInputs(out);
+    });
+}
+
+int spock_status(spock_solver sv, long instance, int *status, long *iters, double *seconds) {
+    return guard([&] {
+        auto *s = solver(sv);
+        if (instance < 0 || instance >= s->eng->batch()) throw std::invalid_argument("[Cache] instance out of range");
+        if (status) *status = s->status[instance];
+        if (iters) *iters = s->iters[instance];
+        if (seconds) *seconds = s->seconds;
+    });
+}
+
+int spock_counters(spock_solver sv, long *out7) {
+    return guard([&] {
+        auto *s = solver(sv);
+        need(out7, "out");
+        s->eng->getCounters(out7);
+    });
+}
+
+int spock_reset(spock_solver sv) {
+    return guard([&] {
+        auto *s = solver(sv);
+        s->eng->zeroIterate();
+        std::fill(s->status.begin(), s->status.end(), SPOCK_NOT_RUN);
+    });
+}
+
+int spock_op(spock_solver sv, const double *prim, double *dual) {
+    return guard([&] {
+        auto *s = solver(sv);
+        need(prim, "prim");
+        need(dual, "dual");
+        s->eng->op(prim, dual);
+    });
+}
+
+int spock_adj(spock_solver sv, const double *dual, double *prim) {
+    return guard([&] {
+        auto *s = solver(sv);
+        need(prim, "prim");
+        need(dual, "dual");
+        s->eng->adj(dual, prim);
+    });
+}
+
+int spock_cp_step(spock_solver sv, const double *x0, const double *z, double *cand) {
+    return guard([&] {
+        auto *s = solver(sv);
+        need(x0, "x0");
+        need(z, "z");
+        need(cand, "cand");
+        s->eng->cpStep(x0, z, cand);
+    });
+}
+
+int spock_apply_m(spock_solver sv, const double *z, double *mz) {
+    return guard([&] {
+        auto *s = solver(sv);
+        need(z, "z");
+        need(mz, "mz");
+        s->eng->applyM(z, mz);
+    });
+}
+
+int spock_kernel_time(spock_solver sv, const char *which, int reps, double *ms, long *bytes) {
+    return guard([&] {
+        auto *s = solver(sv);
+        need(which, "which");
+        if (ms) *ms = s->eng->kernelMs(which, reps < 1 ? 1 : reps);
+        if (bytes) *bytes = s->eng->bytesPerRoundAlgorithmic(which);
+    });
+}
+
+int spock_round_time(spock_solver sv, int rounds, double *ms) {
+    return guard([&] {
+        auto *s = solver(sv);
+        float f = 0;
+        s->eng->timedRounds(rounds < 1 ? 1 : rounds, &f);
+        if (ms) *ms = f;
+    });
+}
+
+int spock_run_stats(spock_solver sv, long *rounds, long *launches) {
+    return guard([&] {
+        auto *s = solver(sv);
+        if (rounds) *rounds = s->eng->lastRounds();
+        if (launches) *launches = s->eng->lastLaunches();
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,954 @@
+// SPOCK engine: SuperMann/CP control on the device and the host loop (see engine.cuh).
+//
+// A SuperMann solve (src/cache.cuh:1008-1132) is run as a sequence of identical "rounds".
+// In every round each instance evaluates T at its current point Z (one CP step), forms the
+// residual r = Z - T(Z) and M r (one L + L* pair), and a per-instance controller decides
+// the next point from the reference's rules:
+//   phase A (outer iteration start): error check every 25 outer iterations, w = ||r||_M,
+//            Anderson direction, then K0 (blind) or the start of the line search;
+//   phase B (line search step tau): K1 (educated), K2 (safeguard), backtrack, or K3 (restore).
+// Both phases need exactly one T evaluation and one M application per round, so a batch of
+// instances in different phases still runs one fixed sequence of launches, which is captured
+// once as a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+
+#include "engine.cuh"
+#include "kernels.cuh"
+
+namespace spock {
+
+#define CK(x)                                                                                      \
+    do {                                                                                           \
+        cudaError_t e_ = (x);                                                                      \
+        if (e_ != cudaSuccess)                                                                     \
+            throw std::runtime_error(std::string("CUDA error ") + cudaGetErrorString(e_) + " at " + \
+                                     __FILE__ + ":" + std::to_string(__LINE__));                   \
+    } while (0)
+
+constexpr int kMaxAnderson = 8;
+constexpr int kNV0 = 5;  // r.Mr, max|Mr|, Mr.d, c.c, c.r ; then c.R_s and R_s.r per slot
+
+enum Action { kActNone = 0, kActFinish = 1, kActAK0 = 2, kActALs = 3, kActBK1 = 4, kActBK2 = 5, kActBK3 = 6, kActBBt = 7,
+              kActCp = 8 };
+
+// ------------------------------------------------------------------------------------------ reductions
+template <typename T>
+struct RedArgs {
+    const T *R, *MR, *D, *RPREV, *ANDR;
+    const int *phase, *status;
+    double *part;
+    int m, nv, chunks, algo;
+    long rowsPerChunk;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_reduce(const Dims Dm, const RedArgs<T> A) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    double *sred = reinterpret_cast<double *>(smraw);  // [nv][lanes][TB]
+    const int B = Dm.B;
+    const int TB = B >= 32 ? 32 : B;
+    const int lb = threadIdx.x % TB, lane = threadIdx.x / TB, lanes = kRedThreads / TB;
+    const bool laneOk = lane < lanes;
+    const int b = blockIdx.x * TB + lb;
+    const bool act = laneOk && b < B;
+    const int chunk = blockIdx.y;
+    const long k0 = (long)chunk * A.rowsPerChunk;
+    const long k1 = k0 + A.rowsPerChunk < Dm.sZ ? k0 + A.rowsPerChunk : Dm.sZ;
+    T acc[kNV0 + 2 * kMaxAnderson];
+    for (int v = 0; v < A.nv; v++) acc[v] = 0;
+    T amax = 0;
+    const int ph = act ? A.phase[b] : 1;
+    const bool running = act && A.status[b] == -1;
+    const bool wantA = running && A.algo == kSpock && ph == 0;
+    const bool wantB = running && A.algo == kSpock && ph == 1;
+    if (running) {
+        for (long k = k0 + lane; k < k1; k += lanes) {
+            const size_t o = ix(k, B, b);
+            const T r = A.R[o], mr = A.MR[o];
+            acc[0] += r * mr;
+            amax = fmax(amax, fabs(mr));
+            if (wantB) acc[2] += mr * A.D[o];
+            if (wantA) {
+                const T c = r - A.RPREV[o];
+                acc[3] += c * c;
+                acc[4] += c * r;
+                for (int s = 0; s < A.m; s++) {
+                    const T a = A.ANDR[(size_t)s * Dm.sZ * B + o];
+                    acc[kNV0 + s] += c * a;
+                    acc[kNV0 + A.m + s] += a * r;
+                }
+            }
+        }
+    }
+    acc[1] = amax;
+    if (laneOk)
+        for (int v = 0; v < A.nv; v++) sred[(v * lanes + lane) * TB + lb] = (double)acc[v];
+    __syncthreads();
+    if (act && lane == 0)
+        for (int v = 0; v < A.nv; v++) {
+            double s = 0;
+            for (int l = 0; l < lanes; l++) {
+                const double x = sred[(v * lanes + l) * TB + lb];
+                s = (v == 1) ? fmax(s, x) : s + x;
+            }
+            A.part[((size_t)chunk * A.nv + v) * B + b] = s;
+        }
+}
+
+// ------------------------------------------------------------------------------------------ controller
+struct CtlArgs {
+    DevState S;
+    const double *part;
+    int chunks, nv, m, algo;
+    double gamma, tolAbs, tolRel;
+    long maxOuter, maxInner;
+    double ridge;
+};
+
+// Solve the m x m SPD system G g = h (FP64 Cholesky with a small ridge); false on breakdown.
+__device__ bool solveGram(const double *G, const double *h, int m, double ridge, double *g) {
+    double L[kMaxAnderson * kMaxAnderson];
+    double dmax = 0;
+    for (int i = 0; i < m; i++) dmax = fmax(dmax, G[i * m + i]);
+    if (!(dmax > 0)) return false;
+    for (int j = 0; j < m; j++) {
+        double s = G[j * m + j] + ridge * dmax;
+        for (int k = 0; k < j; k++) s -= L[j * m + k] * L[j * m + k];
+        if (!(s > 0)) return false;
+        const double d = sqrt(s);
+        L[j * m + j] = d;
+        for (int i = j + 1; i < m; i++) {
+            double a = G[i * m + j];
+            for (int k = 0; k < j; k++) a -= L[i * m + k] * L[j * m + k];
+            L[i * m + j] = a / d;
+        }
+    }
+    double y[kMaxAnderson];
+    for (int i = 0; i < m; i++) {
+        double a = h[i];
+        for (int k = 0; k < i; k++) a -= L[i * m + k] * y[k];
+        y[i] = a / L[i * m + i];
+    }
+    for (int i = m - 1; i >= 0; i--) {
+        double a = y[i];
+        for (int k = i + 1; k < m; k++) a -= L[k * m + i] * g[k];
+        g[i] = a / L[i * m + i];
+    }
+    for (int i = 0; i < m; i++)
+        if (!isfinite(g[i])) return false;
+    return true;
+}
+
+__global__ void k_control(const int B, const CtlArgs A) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    const DevState &S = A.S;
+    if (S.status[b] != -1) {
+        S.action[b] = kActNone;
+        return;
+    }
+    double v[kNV0 + 2 * kMaxAnderson];
+    for (int k = 0; k < A.nv; k++) {
+        double s = 0;
+        for (int c = 0; c < A.chunks; c++) {
+            const double x = A.part[((size_t)c * A.nv + k) * B + b];
+            s = (k == 1) ? fmax(s, x) : s + x;
+        }
+        v[k] = s;
+    }
+    const double c0 = .99, c1 = .99, c2 = .99, beta = .5, sigma = .1, lambda = 1.;
+    const int m = A.m;
+    // error check (cache.cuh:909-961): r/gamma - [L* r_d; L r_p] = (M r)/gamma
+    auto errorCheck = [&](int idx) {
+        if (idx % 25 != 0) return;
+        const double e = v[1] / A.gamma;
+        if (S.errInit[b]) {
+            S.tol[b] = fmax(A.tolAbs, A.tolRel * e);
+            S.errInit[b] = 0;
+        } else {
+            S.err[b] = e;
+            int st = -1;
+            if (e <= S.tol[b]) st = 0;
+            if (A.maxOuter && idx >= A.maxOuter) st = 1;
+            if (*S.timeUp && idx % 1000 == 0) st = 2;
+            if (!isfinite(e)) st = 3;
+            if (st != -1) {
+                S.status[b] = st;
+                S.iters[b] = idx;
+            }
+        }
+    };
+    S.calls[b] += 1;
+    if (A.algo == kCp) {
+        errorCheck(S.iOut[b]);
+        S.iOut[b] += 1;
+        S.action[b] = kActCp;
+        return;
+    }
+    if (S.phase[b] == 0) {
+        const int iOut = S.iOut[b];
+        errorCheck(iOut);
+        if (S.status[b] != -1) {
+            S.action[b] = kActFinish;
+            return;
+        }
+        const double w = sqrt(fmax(v[0], 0.));
+        S.w[b] = w;
+        // Anderson (cache.cuh:860-904) on a ring of m physical slots: the new column
+        // c = r - r_prev replaces the oldest slot h; G is the Gram matrix of the slots.
+        const int h = S.head[b];
+        double *G = S.G + (size_t)b * kMaxAnderson * kMaxAnderson;
+        double rhs[kMaxAnderson];
+        for (int s = 0; s < m; s++) {
+            if (s == h) continue;
+            G[h * m + s] = G[s * m + h] = v[kNV0 + s];
+            rhs[s] = v[kNV0 + m + s];
+        }
+        G[h * m + h] = v[3];
+        rhs[h] = v[4];
+        double *gam = S.gamma + (size_t)b * kMaxAnderson;
+        int use = 0;
+        if (iOut >= m) use = solveGram(G, rhs, m, A.ridge, gam) ? 1 : 0;
+        if (!use)
+            for (int s = 0; s < m; s++) gam[s] = 0;
+        S.useAnd[b] = use;
+        S.head[b] = (h + 1) % m;
+        if (w <= c0 * S.zeta[b]) {  // K0: blind update
+            S.zeta[b] = w;
+            S.k0[b] += 1;
+            S.iOut[b] = iOut + 1;
+            S.action[b] = kActAK0;
+        } else {  // line search starts at tau = 1
+            S.tau[b] = 1.;
+            S.iIn[b] = 0;
+            S.phase[b] = 1;
+            S.action[b] = kActALs;
+        }
+        return;
+    }
+    // phase B: line search step
+    const double w = S.w[b], tau = S.tau[b];
+    const double wT = sqrt(fmax(v[0], 0.));
+    const int iOut = S.iOut[b];
+    if (w <= S.wSafe[b] && wT <= c1 * w) {  // K1: educated update
+        S.wSafe[b] = wT + pow(c2, (double)iOut);
+        S.k1[b] += 1;
+        S.phase[b] = 0;
+        S.iOut[b] = iOut + 1;
+        S.action[b] = kActBK1;
+        return;
+    }
+    const double rho = wT * wT - tau * v[2];  // r'M(tau d) = tau (M r)'d
+    if (rho >= sigma * wT * w) {               // K2: safeguard
+        S.coef[b] = lambda * rho / (wT * wT);
+        S.k2[b] += 1;
+        S.phase[b] = 0;
+        S.iOut[b] = iOut + 1;
+        S.action[b] = kActBK2;
+        return;
+    }
+    S.tau[b] = tau * beta;
+    S.k2bt[b] += 1;
+    if (S.iIn[b] >= A.maxInner - 1) {  // K3: restore the backed-up T(z)
+        S.k3[b] += 1;
+        S.phase[b] = 0;
+        S.iOut[b] = iOut + 1;
+        S.action[b] = kActBK3;
+        return;
+    }
+    S.iIn[b] += 1;
+    S.action[b] = kActBBt;
+}
+
+// ------------------------------------------------------------------------------------------ vector update
+template <typename T>
+struct UpdArgs {
+    T *Z, *CAND, *R, *PREV, *RPREV, *BACKUP, *D, *ANDR, *ANDZ;
+    const int *action, *head, *useAnd;
+    const double *gamma, *tau, *coef;
+    int m;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_update(const Dims Dm, const UpdArgs<T> A) {
+    const int B = Dm.B;
+    const size_t total = (size_t)Dm.sZ * B;
+    const size_t slot = (size_t)Dm.sZ * B;
+    for (size_t o = (size_t)blockIdx.x * blockDim.x + threadIdx.x; o < total; o += (size_t)gridDim.x * blockDim.x) {
+        const int b = (int)(o % B);
+        const int act = A.action[b];
+        switch (act) {
+            case kActAK0:
+            case kActALs: {
+                const T z = A.Z[o], r = A.R[o], c = A.CAND[o];
+                const T dr = r - A.RPREV[o];
+                const T dzr = (z - A.PREV[o]) - dr;
+                const int m = A.m;
+                const int h = (A.head[b] + m - 1) % m;  // slot written this round (head already advanced)
+                T d = -r;
+                if (A.useAnd[b]) {
+                    const double *g = A.gamma + (size_t)b * kMaxAnderson;
+                    for (int s = 0; s < m; s++) d -= T(g[s]) * (s == h ? dzr : A.ANDZ[s * slot + o]);
+                }
+                A.ANDR[h * slot + o] = dr;
+                A.ANDZ[h * slot + o] = dzr;
+                A.D[o] = d;
+                A.PREV[o] = z;
+                A.RPREV[o] = r;
+                A.BACKUP[o] = c;
+                A.Z[o] = z + d;
+                break;
+            }
+            case kActFinish:
+            case kActCp:
+                A.Z[o] = A.CAND[o];
+                break;
+            case kActBK2:
+                A.Z[o] = A.PREV[o] - T(A.coef[b]) * A.R[o];
+                break;
+            case kActBK3:
+                A.Z[o] = A.BACKUP[o];
+                break;
+            case kActBBt:
+                A.Z[o] = A.PREV[o] + T(A.tau[b]) * A.D[o];
+                break;
+            default:
+                break;
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------ small kernels
+template <typename T>
+__global__ void k_fill(T *p, size_t n, T v) {
+    for (size_t o = (size_t)blockIdx.x * blockDim.x + threadIdx.x; o < n; o += (size_t)gridDim.x * blockDim.x) p[o] = v;
+}
+
+template <typename T>
+__global__ void k_copy(T *dst, const T *src, size_t n) {
+    for (size_t o = (size_t)blockIdx.x * blockDim.x + threadIdx.x; o < n; o += (size_t)gridDim.x * blockDim.x) dst[o] = src[o];
+}
+
+template <typename T>
+__global__ void k_scale_x0(T *x0s, const T *x0, const T *scal, int nx, int B) {
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= nx * B) return;
+    const int c = o / B;
+    x0s[o] = x0[o] * scal[c];
+}
+
+__global__ void k_init_state(DevState S, int B, int warm) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    S.phase[b] = 0; S.iOut[b] = 0; S.iIn[b] = 0; S.status[b] = -1; S.errInit[b] = 1; S.action[b] = kActNone;
+    S.head[b] = 0; S.useAnd[b] = 0; S.iters[b] = 0;
+    S.k0[b] = S.k1[b] = S.k2[b] = S.k2bt[b] = S.k3[b] = S.calls[b] = 0;
+    S.tau[b] = 0; S.zeta[b] = INFINITY; S.w[b] = INFINITY; S.wSafe[b] = INFINITY; S.tol[b] = 0; S.err[b] = INFINITY;
+    S.coef[b] = 0;
+    for (int k = 0; k < kMaxAnderson * kMaxAnderson; k++) S.G[(size_t)b * kMaxAnderson * kMaxAnderson + k] = 0;
+    for (int k = 0; k < kMaxAnderson; k++) S.gamma[(size_t)b * kMaxAnderson + k] = 0;
+    if (b == 0) { *S.timeUp = 0; }
+}
+
+__global__ void k_count_active(const int *status, int B, int *out) {
+    __shared__ int cnt;
+    if (threadIdx.x == 0) cnt = 0;
+    __syncthreads();
+    int c = 0;
+    for (int b = threadIdx.x; b < B; b += blockDim.x) c += status[b] == -1;
+    atomicAdd(&cnt, c);
+    __syncthreads();
+    if (threadIdx.x == 0) *out = cnt;
+}
+
+// ------------------------------------------------------------------------------------------ engine
+template <typename T>
+class Engine final : public EngineBase {
+public:
+    Engine(const HostProblem &hp, const Options &opt, long batch, int device) {
+        hp_ = hp;
+        B_ = batch;
+        opt_ = opt;
+        if (batch < 1) throw std::invalid_argument("[Cache] batch must be >= 1");
+        if (opt.anderson < 1 || opt.anderson > kMaxAnderson)
+            throw std::invalid_argument("[Cache] Anderson buffer must be in [1, " + std::to_string(kMaxAnderson) + "]");
+        if (hp.costNonleaf == kCostLinear || hp.costLeaf == kCostLinear)
+            throw std::invalid_argument("[Cache] linear costs are not supported by the GB300 kernels yet");
+        if ((hp.conNonleaf != kConNone && hp.conNonleaf != kConRectangle) ||
+            (hp.conLeaf != kConNone && hp.conLeaf != kConRectangle))
+            throw std::invalid_argument("[Cache] polyhedral constraints are not supported by the GB300 kernels yet");
+        CK(cudaSetDevice(device));
+        CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+        buildDims();
+        upload();
+        allocate();
+        raiseSharedLimits();
+    }
+
+    ~Engine() override {
+        if (graph_) cudaGraphExecDestroy(graph_);
+        for (void *p : allocs_) cudaFree(p);
+        if (hostActive_) cudaFreeHost(hostActive_);
+        if (stream_) cudaStreamDestroy(stream_);
+    }
+
+    int precisionBits() const override { return sizeof(T) * 8; }
+    double lastSeconds() const override { return lastSeconds_; }
+
+    void setInitialStates(const double *x0, long count) override {
+        checkCount(count);
+        std::vector<T> h((size_t)D_.nx * B_);
+        for (long b = 0; b < B_; b++)
+            for (int c = 0; c < D_.nx; c++) h[(size_t)c * B_ + b] = (T)(x0[(b % count) * D_.nx + c] * hp_.scaling[c]);
+        CK(cudaMemcpyAsync(x0s_, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, stream_));
+    }
+
+    void setInitialStatesDevice(const void *x0, long count) override {
+        checkCount(count);
+        if (count != B_) throw std::invalid_argument("[Cache] device initial states must cover the whole batch");
+        // x0 is [nx][B] (element-major) in T precision; scale on the device
+        k_scale_x0<T><<<(D_.nx * (int)B_ + 255) / 256, 256, 0, stream_>>>(x0s_, (const T *)x0, scal_, D_.nx, (int)B_);
+        CK(cudaGetLastError());
+    }
+
+    void setIterate(const double *z, long count) override {
+        checkCount(count);
+        std::vector<T> h((size_t)D_.sZ * B_);
+        for (long b = 0; b < B_; b++) {
+            const double *zb = z + (size_t)(b % count) * D_.sZ;
+            for (long k = 0; k < D_.sZ; k++) h[(size_t)k * B_ + b] = (T)zb[k];
+        }
+        CK(cudaMemcpyAsync(Z_, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, stream_));
+        CK(cudaStreamSynchronize(stream_));
+    }
+
+    void zeroIterate() override {
+        fill(Z_, (size_t)D_.sZ * B_, T(0));
+    }
+
+    int run(Algo algo, bool warm) override {
+        const auto t0 = std::chrono::steady_clock::now();
+        const size_t nz = (size_t)D_.sZ * B_;
+        if (!warm) fill(Z_, nz, T(0));
+        if (algo == kSpock) {
+            if (warm) {  // cache.cuh:624-628: prev := z (the residual memory starts at zero)
+                copy(PREV_, Z_, nz);
+                fill(RPREV_, nz, T(0));
+            } else {     // cache.cuh:629-631: prev := ones, residual_prev := ones
+                fill(PREV_, nz, T(1));
+                fill(RPREV_, nz, T(1));
+            }
+            fill(ANDR_, nz * opt_.anderson, T(0));
+            fill(ANDZ_, nz * opt_.anderson, T(0));
+        }
+        k_init_state<<<((int)B_ + 127) / 128, 128, 0, stream_>>>(S_, (int)B_, warm ? 1 : 0);
+        CK(cudaGetLastError());
+        int rounds = 0, polls = 0;
+        long launches = (algo == kSpock ? 5 : 2) + 1;  // buffer fills + state init
+        const int poll = B_ > 1 ? 10 : 25;
+        if (algo == kSpock) {
+            ensureGraph();
+            for (;;) {
+                CK(cudaGraphLaunch(graph_, stream_));
+                rounds++;
+                launches += launchesPerRound();
+                if (rounds % poll == 0) {
+                    polls++;
+                    if (activeCount(t0) == 0) break;
+                }
+            }
+        } else {
+            for (;;) {
+                teval();
+                const bool check = rounds % 25 == 0;
+                if (check) applyMres();
+                reduceLaunch(kCp, check);
+                controlLaunch(kCp);
+                updateLaunch();
+                rounds++;
+                launches += (D_.ns - 1) * 2 + 2 + (check ? 3 : 2) + 1;
+                if (rounds % poll == 0) {
+                    polls++;
+                    if (activeCount(t0) == 0) break;
+                }
+            }
+        }
+        lastRounds_ = rounds;
+        lastLaunches_ = launches + polls;
+        CK(cudaStreamSynchronize(stream_));
+        lastSeconds_ = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        return rounds;
+    }
+
+    void getIterate(long inst, double *out) override {
+        if (inst < 0 || inst >= B_) throw std::invalid_argument("[Cache] instance out of range");
+        std::vector<T> h((size_t)D_.sZ * B_);
+        CK(cudaMemcpyAsync(h.data(), Z_, h.size() * sizeof(T), cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+        for (long k = 0; k < D_.sZ; k++) out[k] = (double)h[(size_t)k * B_ + inst];
+    }
+
+    void getIterates(double *out) override {
+        std::vector<T> h((size_t)D_.sZ * B_);
+        CK(cudaMemcpyAsync(h.data(), Z_, h.size() * sizeof(T), cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+        for (long b = 0; b < B_; b++)
+            for (long k = 0; k < D_.sZ; k++) out[(size_t)b * D_.sZ + k] = (double)h[(size_t)k * B_ + b];
+    }
+
+    void getFirstInputs(double *out) override {
+        std::vector<T> h((size_t)D_.nu * B_);
+        CK(cudaMemcpyAsync(h.data(), Z_, h.size() * sizeof(T), cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+        for (long b = 0; b < B_; b++)
+            for (int c = 0; c < D_.nu; c++) out[(size_t)b * D_.nu + c] = (double)h[(size_t)c * B_ + b] / hp_.scaling[D_.nx + c];
+    }
+
+    void getStatus(int *status, long *iters) override {
+        std::vector<int> st(B_), it(B_);
+        CK(cudaMemcpyAsync(st.data(), S_.status, B_ * sizeof(int), cudaMemcpyDeviceToHost, stream_));
+        CK(cudaMemcpyAsync(it.data(), S_.iters, B_ * sizeof(int), cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+        for (long b = 0; b < B_; b++) {
+            if (status) status[b] = st[b];
+            if (iters) iters[b] = it[b];
+        }
+    }
+
+    void getCounters(long *out) override {
+        int *ptrs[7] = {S_.k0, S_.k1, S_.k2, S_.k2bt, S_.k3, S_.calls, S_.iters};
+        for (int k = 0; k < 7; k++) {
+            int v = 0;
+            CK(cudaMemcpyAsync(&v, ptrs[k], sizeof(int), cudaMemcpyDeviceToHost, stream_));
+            CK(cudaStreamSynchronize(stream_));
+            out[k] = v;
+        }
+    }
+
+    void op(const double *prim, double *dual) override {
+        uploadSlice(W1_, prim, 0, D_.sPrim);
+        OpArgs<T> A = blankArgs();
+        A.in1 = W1_; A.a1 = 1; A.cL = 1; A.out = W2_;
+        launchLop<2>(A);
+        downloadSlice(W2_, dual, D_.sPrim, D_.sDual);
+    }
+
+    void adj(const double *dual, double *prim) override {
+        uploadSlice(W1_, dual, D_.sPrim, D_.sDual);
+        OpArgs<T> A = blankArgs();
+        A.in1 = W1_; A.a1 = 1; A.cL = 1; A.out = W2_;
+        launchLstar<2>(A);
+        downloadSlice(W2_, prim, 0, D_.sPrim);
+    }
+
+    void cpStep(const double *x0, const double *z, double *cand) override {
+        setInitialStates(x0, 1);
+        uploadSlice(Z_, z, 0, D_.sZ);
+        teval();
+        downloadSlice(CAND_, cand, 0, D_.sZ);
+    }
+
+    void applyM(const double *z, double *mz) override {
+        // M z through the residual kernels with CAND = 0, so r = z
+        uploadSlice(Z_, z, 0, D_.sZ);
+        fill(CAND_, (size_t)D_.sZ * B_, T(0));
+        applyMres();
+        downloadSlice(MR_, mz, 0, D_.sZ);
+    }
+
+    double kernelMs(const char *which, int reps) override {
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        std::string w(which);
+        auto once = [&]() {
+            if (w == "lop") launchLop<0>(tevalLopArgs());
+            else if (w == "lstar") launchLstar<0>(tevalLstarArgs());
+            else if (w == "mlop") launchLop<1>(mLopArgs());
+            else if (w == "mlstar") launchLstar<1>(mLstarArgs());
+            else if (w == "reduce") reduceLaunch(kSpock, true);
+            else if (w == "update") updateLaunch();
+            else if (w == "dyn") dynamics();
+            else if (w == "teval") teval();
+            else if (w == "round") roundSpock();
+            else throw std::invalid_argument("unknown kernel " + w);
+        };
+        once();
+        CK(cudaEventRecord(e0, stream_));
+        for (int r = 0; r < reps; r++) once();
+        CK(cudaEventRecord(e1, stream_));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return ms / reps;
+    }
+
+    void timedRounds(int rounds, float *ms) override {
+        ensureGraph();
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        CK(cudaEventRecord(e0, stream_));
+        for (int r = 0; r < rounds; r++) CK(cudaGraphLaunch(graph_, stream_));
+        CK(cudaEventRecord(e1, stream_));
+        CK(cudaEventSynchronize(e1));
+        CK(cudaEventElapsedTime(ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+
+    // Algorithmic bytes per launch: distinct matrix bytes once + vector elements read and
+    // written once, for all B instances.
+    long bytesPerRoundAlgorithmic(const char *which) const override {
+        const std::string w(which);
+        const long s = sizeof(T), B = B_;
+        const long n = D_.n, nnl = D_.nnl, nl = D_.nl, nx = D_.nx, nu = D_.nu;
+        const long matL = s * (n * (nx * nx + nu * nu) + nx * nx);          // sqrtQ, sqrtR, leaf sqrtQ
+        const long matK = s * nnl * (long)D_.nd * D_.nd;                     // NNtr
+        if (w == "lop") return matL + s * B * (2 * D_.sPrim + 2 * D_.sDual);  // reads 2 prim + dual, writes dual
+        if (w == "lstar") return matL + matK + s * B * (D_.sDual + 2 * D_.sPrim);
+        if (w == "mlop") return matL + s * B * (2 * D_.sPrim + 2 * D_.sDual + 2 * D_.sDual);
+        if (w == "mlstar") return matL + s * B * (2 * D_.sDual + 2 * D_.sPrim + 2 * D_.sPrim);
+        if (w == "update") return s * B * D_.sZ * (5 + 7 + (opt_.anderson - 1));
+        if (w == "reduce") return s * B * D_.sZ * (3 + opt_.anderson);
+        if (w == "dyn") {
+            const long mats = s * (n * (nu * nx + nx * nu + nx * nx + nx * (nx + nu)) + nnl * (nu * nx + nu * nu));
+            return mats + s * B * (4 * (nx * n + nu * nnl));
+        }
+        (void)nl;
+        return 0;
+    }
+
+    int launchesPerRound() const override { return 2 * (D_.ns - 1) + 2 + 2 + 3; }
+
+private:
+    Options opt_;
+    Dims D_{};
+    DevProblem<T> P_{};
+    DevState S_{};
+    cudaStream_t stream_ = nullptr;
+    cudaGraphExec_t graph_ = nullptr;
+    std::vector<void *> allocs_;
+    T *Z_ = nullptr, *CAND_ = nullptr, *R_ = nullptr, *MR_ = nullptr, *PREV_ = nullptr, *RPREV_ = nullptr;
+    T *BACKUP_ = nullptr, *DIR_ = nullptr, *ANDR_ = nullptr, *ANDZ_ = nullptr, *Q_ = nullptr, *DD_ = nullptr;
+    T *x0s_ = nullptr, *W1_ = nullptr, *W2_ = nullptr, *scal_ = nullptr;
+    double *part_ = nullptr;
+    int *hostActive_ = nullptr, *devActive_ = nullptr;
+    int chunks_ = 1, nv_ = 0;
+    long rowsPerChunk_ = 1;
+    double lastSeconds_ = 0;
+    std::vector<int> stageFrom_, stageCount_;
+
+    void checkCount(long count) const {
+        if (count < 1 || count > B_) throw std::invalid_argument("[Cache] instance count out of range");
+    }
+
+    template <typename U>
+    U *dalloc(size_t n) {
+        void *p = nullptr;
+        CK(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(U)));
+        allocs_.push_back(p);
+        return (U *)p;
+    }
+
+    template <typename U>
+    const U *upvec(const std::vector<double> &v) {
+        if (v.empty()) return nullptr;
+        std::vector<U> h(v.begin(), v.end());
+        U *d = dalloc<U>(h.size());
+        CK(cudaMemcpy(d, h.data(), h.size() * sizeof(U), cudaMemcpyHostToDevice));
+        return d;
+    }
+
+    const int *upidx(const std::vector<long> &v) {
+        std::vector<int> h(v.begin(), v.end());
+        int *d = dalloc<int>(h.size());
+        CK(cudaMemcpy(d, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice));
+        return d;
+    }
+
+    void buildDims() {
+        const HostProblem &p = hp_;
+        Dims &D = D_;
+        D.n = (int)p.numNodes; D.nnl = (int)p.numNonleaf; D.nl = (int)p.numLeaf; D.ns = (int)p.numStages;
+        D.nx = (int)p.nx; D.nu = (int)p.nu; D.nxu = D.nx + D.nu; D.ne = (int)p.numEvents;
+        D.yD = (int)p.yDim; D.nd = (int)p.nullDim;
+        D.costNl = p.costNonleaf; D.costL = p.costLeaf; D.conNl = p.conNonleaf; D.conL = p.conLeaf;
+        D.affine = p.affine ? 1 : 0;
+        D.dIII = (int)p.dimIII; D.dIV = (int)p.dimIV; D.dV = (int)p.dimV; D.dVI = (int)p.dimVI;
+        D.oX = p.sizeU; D.oY = D.oX + p.sizeX; D.oT = D.oY + p.sizeY; D.oS = D.oT + p.sizeT; D.sPrim = p.sizePrim;
+        D.oI = p.sizePrim; D.oII = D.oI + p.sizeI; D.oIII = D.oII + p.sizeII; D.oIV = D.oIII + p.sizeIII;
+        D.oV = D.oIV + p.sizeIV; D.oVI = D.oV + p.sizeV; D.sDual = p.sizeDual; D.sZ = p.sizeIterate();
+        D.B = (int)B_;
+        D.TB = B_ >= 32 ? 32 : (int)B_;
+        for (long s = 0; s < p.numStages; s++) {
+            stageFrom_.push_back((int)p.stageFrom[s]);
+            stageCount_.push_back((int)(p.stageTo[s] - p.stageFrom[s] + 1));
+        }
+        if (D.nd > 64 || D.nx > 4096) throw std::invalid_argument("[Cache] problem dimensions exceed kernel limits");
+    }
+
+    void upload() {
+        const HostProblem &p = hp_;
+        P_.anc = upidx(p.ancestors);
+        P_.chFrom = upidx(p.childFrom);
+        P_.numCh = upidx(p.numChildren);
+        P_.BTr = upvec<T>(p.BTr); P_.AB = upvec<T>(p.AB); P_.K = upvec<T>(p.K); P_.ABKTr = upvec<T>(p.ABKTr);
+        P_.APB = upvec<T>(p.APB); P_.chol = upvec<T>(p.lowChol); P_.e = upvec<T>(p.e); P_.Pe = upvec<T>(p.Pe);
+        P_.sqrtQ = upvec<T>(p.sqrtQ); P_.sqrtR = upvec<T>(p.sqrtR); P_.q = upvec<T>(p.q); P_.r = upvec<T>(p.r);
+        P_.trans = upvec<T>(p.translation);
+        P_.lSqrtQ = upvec<T>(p.leafSqrtQ); P_.lq = upvec<T>(p.leafQ); P_.lTrans = upvec<T>(p.leafTranslation);
+        P_.nlLo = upvec<T>(p.nlLower); P_.nlHi = upvec<T>(p.nlUpper); P_.lLo = upvec<T>(p.lLower); P_.lHi = upvec<T>(p.lUpper);
+        P_.NNtr = upvec<T>(p.NNtr); P_.b = upvec<T>(p.b);
+        P_.step = (T)p.stepSize;
+        scal_ = const_cast<T *>(upvec<T>(p.scaling));
+    }
+
+    void allocate() {
+        const size_t nz = (size_t)D_.sZ * B_;
+        Z_ = dalloc<T>(nz); CAND_ = dalloc<T>(nz); R_ = dalloc<T>(nz); MR_ = dalloc<T>(nz);
+        PREV_ = dalloc<T>(nz); RPREV_ = dalloc<T>(nz); BACKUP_ = dalloc<T>(nz); DIR_ = dalloc<T>(nz);
+        ANDR_ = dalloc<T>(nz * opt_.anderson); ANDZ_ = dalloc<T>(nz * opt_.anderson);
+        Q_ = dalloc<T>((size_t)D_.nx * D_.n * B_); DD_ = dalloc<T>((size_t)D_.nu * D_.nnl * B_);
+        x0s_ = dalloc<T>((size_t)D_.nx * B_);
+        W1_ = dalloc<T>(nz); W2_ = dalloc<T>(nz);
+        fill(Z_, nz, T(0)); fill(CAND_, nz, T(0)); fill(R_, nz, T(0)); fill(MR_, nz, T(0));
+        fill(DIR_, nz, T(0)); fill(W1_, nz, T(0)); fill(W2_, nz, T(0)); fill(x0s_, (size_t)D_.nx * B_, T(0));
+        nv_ = kNV0 + 2 * (int)opt_.anderson;
+        const int tiles = (int)((B_ + 31) / 32);
+        const int target = 1216;  // ~8 CTAs per SM
+        chunks_ = std::max(1, std::min<int>(target / tiles, (int)((D_.sZ + 255) / 256)));
+        rowsPerChunk_ = (D_.sZ + chunks_ - 1) / chunks_;
+        part_ = dalloc<double>((size_t)chunks_ * nv_ * B_);
+        const size_t Bi = (size_t)B_;
+        int *ib = dalloc<int>(Bi * 16);
+        S_.phase = ib; S_.iOut = ib + Bi; S_.iIn = ib + 2 * Bi; S_.status = ib + 3 * Bi; S_.errInit = ib + 4 * Bi;
+        S_.action = ib + 5 * Bi; S_.head = ib + 6 * Bi; S_.useAnd = ib + 7 * Bi; S_.iters = ib + 8 * Bi;
+        S_.k0 = ib + 9 * Bi; S_.k1 = ib + 10 * Bi; S_.k2 = ib + 11 * Bi; S_.k2bt = ib + 12 * Bi; S_.k3 = ib + 13 * Bi;
+        S_.calls = ib + 14 * Bi;
+        double *db = dalloc<double>(Bi * (8 + 2 * kMaxAnderson * kMaxAnderson));
+        S_.tau = db; S_.zeta = db + Bi; S_.w = db + 2 * Bi; S_.wSafe = db + 3 * Bi; S_.tol = db + 4 * Bi;
+        S_.err = db + 5 * Bi; S_.coef = db + 6 * Bi; S_.G = db + 8 * Bi;
+        S_.gamma = S_.G + Bi * kMaxAnderson * kMaxAnderson;
+        int *misc = dalloc<int>(4);
+        S_.timeUp = misc; S_.active = misc + 1;
+        devActive_ = misc + 2;
+        CK(cudaMemset(misc, 0, 4 * sizeof(int)));
+        CK(cudaMemset(ib, 0, Bi * 16 * sizeof(int)));
+        CK(cudaMemset(db, 0, Bi * (8 + 2 * kMaxAnderson * kMaxAnderson) * sizeof(double)));
+        CK(cudaMallocHost((void **)&hostActive_, sizeof(int)));
+        k_init_state<<<((int)B_ + 127) / 128, 128, 0, stream_>>>(S_, (int)B_, 0);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(stream_));
+    }
+
+    // Opt in to more than 48 KB of dynamic shared memory where a problem needs it.
+    template <typename K>
+    void optIn(K kernel, size_t bytes) {
+        if (bytes <= 48 * 1024) return;
+        if (bytes > 227 * 1024) throw std::invalid_argument("[Cache] problem too large for the shared-memory tiles");
+        CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    }
+
+    void raiseSharedLimits() {
+        optIn(k_dyn_back<T>, smBack());
+        optIn(k_dyn_fwd<T>, smFwd());
+        optIn(k_lstar<T, 0>, smLstar());
+        optIn(k_lstar<T, 1>, smLstar());
+        optIn(k_lstar<T, 2>, smLstar());
+        optIn(k_lop<T, 0>, smLop());
+        optIn(k_lop<T, 1>, smLop());
+        optIn(k_lop<T, 2>, smLop());
+    }
+
+    size_t smBack() const { return (size_t)(D_.ne * D_.nx + 2 * D_.nu) * D_.TB * sizeof(T); }
+    size_t smFwd() const { return (size_t)(D_.nx + D_.nu) * D_.TB * sizeof(T); }
+    size_t smLstar() const { return (size_t)D_.nd * D_.TB * sizeof(T); }
+    size_t smLop() const { return (size_t)std::max(D_.dIV, D_.dVI) * D_.TB * sizeof(T); }
+
+    void fill(T *p, size_t n, T v) {
+        k_fill<T><<<(int)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, stream_>>>(p, n, v);
+        CK(cudaGetLastError());
+    }
+
+    void copy(T *dst, const T *src, size_t n) {
+        k_copy<T><<<(int)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, stream_>>>(dst, src, n);
+        CK(cudaGetLastError());
+    }
+
+    // host slice [off, off+len) of instance 0 <-> device element-major buffer (B must be 1 for
+    // exact placement; for B > 1 the slice is replicated into every instance)
+    void uploadSlice(T *dst, const double *src, long off, long len) {
+        std::vector<T> h((size_t)len * B_);
+        for (long k = 0; k < len; k++)
+            for (long b = 0; b < B_; b++) h[(size_t)k * B_ + b] = (T)src[k];
+        CK(cudaMemcpyAsync(dst + (size_t)off * B_, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, stream_));
+        CK(cudaStreamSynchronize(stream_));
+    }
+
+    void downloadSlice(const T *src, double *dst, long off, long len) {
+        std::vector<T> h((size_t)len * B_);
+        CK(cudaMemcpyAsync(h.data(), src + (size_t)off * B_, h.size() * sizeof(T), cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+        for (long k = 0; k < len; k++) dst[k] = (double)h[(size_t)k * B_];
+    }
+
+    OpArgs<T> blankArgs() const {
+        OpArgs<T> A{};
+        A.a1 = 1; A.a2 = 0; A.b1 = 1; A.b2 = 0; A.cL = 1;
+        A.x0s = x0s_;
+        return A;
+    }
+
+    OpArgs<T> tevalLstarArgs() const {  // p - gamma L* d, then prox (cache.cuh:748-764)
+        OpArgs<T> A = blankArgs();
+        A.in1 = Z_; A.base1 = Z_; A.cL = -P_.step; A.out = CAND_;
+        return A;
+    }
+    OpArgs<T> tevalLopArgs() const {  // d + gamma L(2 pbar - p), then dual prox (cache.cuh:770-789)
+        OpArgs<T> A = blankArgs();
+        A.in1 = CAND_; A.a1 = 2; A.in2 = Z_; A.a2 = -1; A.base1 = Z_; A.cL = P_.step; A.out = CAND_;
+        return A;
+    }
+    OpArgs<T> mLstarArgs() const {  // r_p - gamma L* r_d, r = Z - CAND
+        OpArgs<T> A = blankArgs();
+        A.in1 = Z_; A.in2 = CAND_; A.a2 = -1; A.base1 = Z_; A.base2 = CAND_; A.b2 = -1; A.cL = -P_.step;
+        A.out = MR_; A.outBase = R_;
+        return A;
+    }
+    OpArgs<T> mLopArgs() const {  // r_d - gamma L r_p
+        OpArgs<T> A = mLstarArgs();
+        return A;
+    }
+
+    dim3 nodeGrid(int nodes) const { return dim3((unsigned)((B_ + D_.TB - 1) / D_.TB), (unsigned)nodes); }
+
+    template <int MODE>
+    void launchLstar(const OpArgs<T> &A) {
+        k_lstar<T, MODE><<<nodeGrid(D_.n), kNodeThreads, smLstar(), stream_>>>(P_, D_, A);
+        CK(cudaGetLastError());
+    }
+
+    template <int MODE>
+    void launchLop(const OpArgs<T> &A) {
+        k_lop<T, MODE><<<nodeGrid(D_.n), kNodeThreads, smLop(), stream_>>>(P_, D_, A);
+        CK(cudaGetLastError());
+    }
+
+    void dynamics() {
+        const int N = D_.ns - 1;
+        const size_t smB = smBack(), smF = smFwd();
+        for (int st = N - 1; st >= 0; st--) {
+            k_dyn_back<T><<<nodeGrid(stageCount_[st]), kNodeThreads, smB, stream_>>>(P_, D_, CAND_, Q_, DD_, stageFrom_[st], st);
+            CK(cudaGetLastError());
+        }
+        for (int st = 0; st < N; st++) {
+            k_dyn_fwd<T><<<nodeGrid(stageCount_[st]), kNodeThreads, smF, stream_>>>(P_, D_, CAND_, DD_, x0s_, stageFrom_[st]);
+            CK(cudaGetLastError());
+        }
+    }
+
+    void teval() {
+        launchLstar<0>(tevalLstarArgs());
+        dynamics();
+        launchLop<0>(tevalLopArgs());
+    }
+
+    void applyMres() {
+        launchLstar<1>(mLstarArgs());
+        launchLop<1>(mLopArgs());
+    }
+
+    void reduceLaunch(Algo algo, bool withData) {
+        RedArgs<T> A{};
+        A.R = R_; A.MR = MR_; A.D = DIR_; A.RPREV = RPREV_; A.ANDR = ANDR_;
+        A.phase = S_.phase; A.status = S_.status; A.part = part_;
+        A.m = (int)opt_.anderson; A.nv = nv_; A.chunks = chunks_; A.algo = algo; A.rowsPerChunk = rowsPerChunk_;
+        if (!withData) {  // CP rounds between error checks: no reduction needed
+            CK(cudaMemsetAsync(part_, 0, sizeof(double) * (size_t)chunks_ * nv_ * B_, stream_));
+            return;
+        }
+        const int TB = B_ >= 32 ? 32 : (int)B_;
+        const int lanes = kRedThreads / TB;
+        const size_t sm = (size_t)nv_ * lanes * TB * sizeof(double);
+        dim3 grid((unsigned)((B_ + TB - 1) / TB), (unsigned)chunks_);
+        k_reduce<T><<<grid, kRedThreads, sm, stream_>>>(D_, A);
+        CK(cudaGetLastError());
+    }
+
+    void controlLaunch(Algo algo) {
+        CtlArgs A{};
+        A.S = S_; A.part = part_; A.chunks = chunks_; A.nv = nv_; A.m = (int)opt_.anderson; A.algo = algo;
+        A.gamma = hp_.stepSize;
+        const double ts = hp_.preconditioned ? hp_.minScaling() : 1.;  // cache.cuh:302-306
+        A.tolAbs = opt_.tolAbs * ts;
+        A.tolRel = opt_.tolRel * ts;
+        A.maxOuter = opt_.maxOuter;
+        A.maxInner = opt_.maxInner;
+        A.ridge = sizeof(T) == 8 ? 1e-13 : 1e-7;
+        k_control<<<((int)B_ + 127) / 128, 128, 0, stream_>>>((int)B_, A);
+        CK(cudaGetLastError());
+    }
+
+    void updateLaunch() {
+        UpdArgs<T> A{};
+        A.Z = Z_; A.CAND = CAND_; A.R = R_; A.PREV = PREV_; A.RPREV = RPREV_; A.BACKUP = BACKUP_; A.D = DIR_;
+        A.ANDR = ANDR_; A.ANDZ = ANDZ_; A.action = S_.action; A.head = S_.head; A.useAnd = S_.useAnd;
+        A.gamma = S_.gamma; A.tau = S_.tau; A.coef = S_.coef; A.m = (int)opt_.anderson;
+        const size_t total = (size_t)D_.sZ * B_;
+        const int grid = (int)std::min<size_t>((total + 255) / 256, 152 * 8);
+        k_update<T><<<grid, 256, 0, stream_>>>(D_, A);
+        CK(cudaGetLastError());
+    }
+
+    void roundSpock() {
+        teval();
+        applyMres();
+        reduceLaunch(kSpock, true);
+        controlLaunch(kSpock);
+        updateLaunch();
+    }
+
+    void ensureGraph() {
+        if (graph_) return;
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+        roundSpock();
+        CK(cudaStreamEndCapture(stream_, &g));
+        CK(cudaGraphInstantiate(&graph_, g, 0));
+        CK(cudaGraphDestroy(g));
+    }
+
+    int activeCount(std::chrono::steady_clock::time_point t0) {
+        if (opt_.maxTimeSecs > 0) {
+            const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            if (el >= opt_.maxTimeSecs) {
+                const int one = 1;
+                CK(cudaMemcpyAsync(S_.timeUp, &one, sizeof(int), cudaMemcpyHostToDevice, stream_));
+            }
+        }
+        k_count_active<<<1, 256, 0, stream_>>>(S_.status, (int)B_, devActive_);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(hostActive_, devActive_, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+        return *hostActive_;
+    }
+};
+
+EngineBase *makeEngine(const HostProblem &hp, const Options &opt, long batch, int precisionBits, int device) {
+    if (precisionBits == 64) return new Engine<double>(hp, opt, batch, device);
+    if (precisionBits == 32) return new Engine<float>(hp, opt, batch, device);
+    throw std::invalid_argument("[Cache] precision must be 32 or 64");
+}
+
+}  // namespace spock

@@ -1,0 +1,111 @@
+// SPOCK solve engine for GB300 (sm_103a): device data, per-iteration kernels, SuperMann
+// controller and the host loop that drives them.
+//
+// Memory layout.  Every iterate-sized vector of a batch of B instances is one array
+// [element][instance]: entry k of instance b lives at k*B + b.  Element order is the
+// reference's iterate layout (cache.cuh:481-497, 529-581):
+//   prim = [u (nu x nonleaf) | x (nx x nodes) | y ((2E+1) x nonleaf) | t (nodes) | s (nodes)]
+//   dual = [I ((2E+1) x nonleaf) | II (nonleaf) | III (nonleaf constraint) |
+//           IV (nonleaf cost, every node incl. root) | V (leaf constraint) | VI (leaf cost)]
+// so with B = 1 it is exactly the reference's vector, and with B > 1 a warp reads 32
+// instances of one element in one coalesced transaction.  Per-node problem matrices are
+// shared by all instances (uniform batch) and read as warp-wide broadcasts.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <string>
+#include <vector>
+
+#include "problem.hpp"
+
+namespace spock {
+
+struct Dims {
+    int n, nnl, nl, ns, nx, nu, nxu, ne, yD, nd;
+    int costNl, costL, conNl, conL, affine;
+    int dIII, dIV, dV, dVI;
+    long oX, oY, oT, oS, sPrim;              // primal offsets
+    long oI, oII, oIII, oIV, oV, oVI, sDual;  // dual offsets, absolute (dual starts at sPrim)
+    long sZ;
+    int B;   // instances
+    int TB;  // instances per CTA in the node kernels
+};
+
+template <typename T>
+struct DevProblem {
+    const int *anc, *chFrom, *numCh;
+    const T *BTr, *AB, *K, *ABKTr, *APB, *chol, *e, *Pe;
+    const T *sqrtQ, *sqrtR, *q, *r, *trans;
+    const T *lSqrtQ, *lq, *lTrans;
+    const T *nlLo, *nlHi, *lLo, *lHi;
+    const T *NNtr, *b;
+    T step;
+};
+
+// out = base + cL * Op(v), v = a1*in1 (+ a2*in2), base = b1*base1 (+ b2*base2).
+template <typename T>
+struct OpArgs {
+    const T *in1, *in2;
+    T a1, a2;
+    const T *base1, *base2;
+    T b1, b2;
+    T cL;
+    T *out;
+    T *outBase;     // when set, base is stored here too (the residual r)
+    const T *x0s;   // scaled initial states, nx x B
+};
+
+struct Options {
+    double tolAbs = 1e-3, tolRel = 0., maxTimeSecs = 0.;
+    long maxOuter = 0, maxInner = 8, anderson = 3;
+};
+
+enum Algo { kSpock = 0, kCp = 1 };
+
+// Per-instance SuperMann / CP state, structure of arrays on the device.
+struct DevState {
+    int *phase, *iOut, *iIn, *status, *errInit, *action, *head, *useAnd, *iters;
+    int *k0, *k1, *k2, *k2bt, *k3, *calls;
+    double *tau, *zeta, *w, *wSafe, *tol, *err, *coef, *G, *gamma;
+    int *timeUp, *active;
+};
+
+class EngineBase {
+public:
+    virtual ~EngineBase() = default;
+    virtual void setInitialStates(const double *x0, long count) = 0;   // host, unscaled, count*nx
+    virtual void setInitialStatesDevice(const void *x0, long count) = 0;  // device, unscaled, T
+    virtual void setIterate(const double *z, long count) = 0;           // host warm start, count*sZ
+    virtual void zeroIterate() = 0;
+    virtual int run(Algo algo, bool warm) = 0;  // returns number of rounds
+    virtual void getIterate(long inst, double *out) = 0;
+    virtual void getIterates(double *out) = 0;  // all, instance-major count*sZ
+    virtual void getFirstInputs(double *out) = 0;  // unscaled u_0, B*nu
+    virtual void getStatus(int *status, long *iters) = 0;
+    virtual void getCounters(long *out7) = 0;  // instance 0: k0,k1,k2,k2bt,k3,calls,iters
+    virtual void op(const double *prim, double *dual) = 0;
+    virtual void adj(const double *dual, double *prim) = 0;
+    virtual void cpStep(const double *x0, const double *z, double *cand) = 0;
+    virtual void applyM(const double *z, double *mz) = 0;
+    virtual int precisionBits() const = 0;
+    virtual double lastSeconds() const = 0;
+    virtual double kernelMs(const char *which, int reps) = 0;  // CUDA-event timing of one kernel
+    virtual void timedRounds(int rounds, float *ms) = 0;
+    virtual long bytesPerRoundAlgorithmic(const char *which) const = 0;
+    virtual int launchesPerRound() const = 0;
+    long lastRounds() const { return lastRounds_; }
+    long lastLaunches() const { return lastLaunches_; }
+    const HostProblem &problem() const { return hp_; }
+    long batch() const { return B_; }
+
+protected:
+    HostProblem hp_;
+    long B_ = 1;
+    long lastRounds_ = 0, lastLaunches_ = 0;
+};
+
+EngineBase *makeEngine(const HostProblem &hp, const Options &opt, long batch, int precisionBits, int device);
+
+}  // namespace spock

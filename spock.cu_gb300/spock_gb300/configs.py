@@ -1,0 +1,107 @@
+"""Seeded synthetic RAOCP workloads (the five benchmark configurations).
+
+Each builder writes a problem folder (data.json + .bt) with `factory` and returns
+(path, x0) where x0 is a (count, nx) array of initial states drawn from the same seed.
+Sizes:
+  config1: 3-state Markov chain, N=4, tau=2 -> 31 nodes; nx=3, nu=2; quadratic costs;
+           box |x|<=5, |u|<=2; AVaR(0.9); x0 ~ U[-1,1]^3; eps=1e-3, Anderson memory 3.
+  config2: 3-state Markov chain, N=10, tau=4 -> 607 nodes; nx=50, nu=20; A_w ~ N(0,1/nx)
+           rescaled to spectral radius 1.05, B_w ~ N(0,1); quadratic-plus-linear costs
+           Q=diag U[1,10], R=diag U[0.1,1], q, r ~ N(0,1); box |x|<=3, |u|<=1; AVaR(0.95);
+           x0 ~ U[-1,1]^50; eps=1e-4, Anderson memory 5.
+  config3: i.i.d. process with 5 equiprobable events, N=8, tau=3 -> 781 nodes; nx=100, nu=40;
+           dynamics generated as config2; quadratic costs; box on x; AVaR(0.9).
+"""
+import os
+
+import numpy as np
+
+from . import factory as F
+
+SOLVER = {
+    "config1": dict(tol=1e-3, anderson=3),
+    "config2": dict(tol=1e-4, anderson=5),
+    "config3": dict(tol=1e-4, anderson=5),
+}
+
+
+def _stable_dynamics(rng, nx, nu, events, radius=1.05):
+    out = []
+    for _ in range(events):
+        A = rng.normal(0., 1. / np.sqrt(nx), size=(nx, nx))
+        A *= radius / max(abs(np.linalg.eigvals(A)))
+        out.append(F.Dynamics(A, rng.standard_normal((nx, nu))))
+    return out
+
+
+def config1(path, seed=0, count=1):
+    rng = np.random.default_rng(seed)
+    ne, nx, nu = 3, 3, 2
+    P = rng.dirichlet(np.ones(ne), size=ne)
+    tree = F.MarkovChain(P, np.ones(ne) / ne, horizon=4, stopping_stage=2).build()
+    dyn = [F.Dynamics(np.eye(nx) + .1 * rng.standard_normal((nx, nx)), rng.standard_normal((nx, nu)))
+           for _ in range(ne)]
+    Q = np.diag(rng.uniform(1., 10., nx))
+    R = np.diag(rng.uniform(.1, 1., nu))
+    lb = np.concatenate((-5. * np.ones(nx), -2. * np.ones(nu)))
+    (F.Factory(tree, nx, nu).with_dynamics_events(dyn)
+     .with_cost_nonleaf(F.CostQuadratic(Q, R))
+     .with_cost_leaf(F.CostQuadratic(Q, leaf=True))
+     .with_constraint_nonleaf(F.Rectangle(lb, -lb))
+     .with_constraint_leaf(F.Rectangle(-5. * np.ones(nx), 5. * np.ones(nx)))
+     .with_risk(F.AVaR(.9))
+     .generate_problem(path))
+    return path, rng.uniform(-1., 1., size=(count, nx))
+
+
+def config2(path, seed=0, count=1, nx=50, nu=20, horizon=10, stopping=4, states=3):
+    rng = np.random.default_rng(seed)
+    P = rng.dirichlet(np.ones(states), size=states)
+    tree = F.MarkovChain(P, np.ones(states) / states, horizon=horizon, stopping_stage=stopping).build()
+    dyn = _stable_dynamics(rng, nx, nu, states)
+    costs = [F.CostQuadraticPlusLinear(np.diag(rng.uniform(1., 10., nx)), rng.standard_normal(nx),
+                                       np.diag(rng.uniform(.1, 1., nu)), rng.standard_normal(nu))
+             for _ in range(states)]
+    leaf = F.CostQuadraticPlusLinear(np.diag(rng.uniform(1., 10., nx)), rng.standard_normal(nx), leaf=True)
+    lb = np.concatenate((-3. * np.ones(nx), -1. * np.ones(nu)))
+    (F.Factory(tree, nx, nu).with_dynamics_events(dyn)
+     .with_cost_nonleaf_events(costs)
+     .with_cost_leaf(leaf)
+     .with_constraint_nonleaf(F.Rectangle(lb, -lb))
+     .with_constraint_leaf(F.Rectangle(-3. * np.ones(nx), 3. * np.ones(nx)))
+     .with_risk(F.AVaR(.95))
+     .generate_problem(path))
+    return path, rng.uniform(-1., 1., size=(count, nx))
+
+
+def config3(path, seed=0, count=1):
+    rng = np.random.default_rng(seed)
+    ne, nx, nu = 5, 100, 40
+    tree = F.IidProcess(np.ones(ne) / ne, horizon=8, stopping_stage=3).build()
+    dyn = _stable_dynamics(rng, nx, nu, ne)
+    costs = [F.CostQuadratic(np.diag(rng.uniform(1., 10., nx)), np.diag(rng.uniform(.1, 1., nu)))
+             for _ in range(ne)]
+    leaf = F.CostQuadratic(np.diag(rng.uniform(1., 10., nx)), leaf=True)
+    lb = np.concatenate((-3. * np.ones(nx), -2. * np.ones(nu)))
+    (F.Factory(tree, nx, nu).with_dynamics_events(dyn)
+     .with_cost_nonleaf_events(costs)
+     .with_cost_leaf(leaf)
+     .with_constraint_nonleaf(F.Rectangle(lb, -lb))
+     .with_constraint_leaf(F.Rectangle(-3. * np.ones(nx), 3. * np.ones(nx)))
+     .with_risk(F.AVaR(.9))
+     .generate_problem(path))
+    return path, rng.uniform(-1., 1., size=(count, nx))
+
+
+BUILDERS = {"config1": config1, "config2": config2, "config3": config3}
+
+
+def cached(name, root, seed=0, count=1, **kw):
+    """Build a configuration once under `root/name_s{seed}` and reuse it afterwards."""
+    path = os.path.join(root, f"{name}_s{seed}" + "".join(f"_{k}{v}" for k, v in sorted(kw.items())), "")
+    if not os.path.exists(os.path.join(path, "data.json")):
+        BUILDERS[name](path, seed=seed, count=1, **kw)
+    rng = np.random.default_rng(seed + 7919)
+    import json
+    nx = json.load(open(os.path.join(path, "data.json")))["numStates"]
+    return path, rng.uniform(-1., 1., size=(count, nx))

@@ -1,0 +1,211 @@
+"""Parity of the CUDA path (through the C ABI) with the FP64 CPU oracle.
+
+Tolerances: FP64 kernels must agree with the oracle to 1e-10 relative (same arithmetic up to
+summation order); FP32 kernels to 2e-5 relative to the vector's scale (single precision).
+Solves are compared on the solution they return: FP64 to 1e-6, FP32 to 1e-3 relative.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden
+
+import spock_gb300 as sg
+
+pytestmark = pytest.mark.gpu
+
+CASES = ["reftest", "cfg1", "qpl"]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    sg.build()
+
+
+def make(path, precision=64, batch=1, tol=1e-3, max_iters=0, anderson=3):
+    t = sg.ScenarioTree(path)
+    d = sg.ProblemData(t)
+    c = (sg.CacheBuilder(t, d).tol(tol).maxIters(max_iters).andersonBuffer(anderson)
+         .precision(precision).batch(batch).build())
+    return t, d, c
+
+
+def x0_of(case, nx):
+    return golden(case, "initialState_d.bt") if case != "reftest" else np.full(nx, 1.1)
+
+
+def rel(a, b):
+    return np.abs(a - b).max() / max(1., np.abs(b).max())
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("precision,tol", [(64, 1e-12), (32, 2e-5)])
+def test_operators(oracle_lib, case, precision, tol):
+    path = os.path.join(GOLDEN, case)
+    t, d, c = make(path, precision)
+    P = oracle_lib.Problem(path)
+    prim = golden(case, "test_primBeforeOp_d.bt")
+    dual = golden(case, "test_dualAfterOpBeforeAdj_d.bt")
+    assert rel(c.op(prim), dual) < tol
+    assert rel(c.adj(dual), golden(case, "test_primAfterAdj_d.bt")) < tol
+    rng = np.random.default_rng(5)
+    z = rng.standard_normal(c.sizeIterate())
+    assert rel(c.applyM(z), np.concatenate((z[:P.size_prim] - P.step * P.adj(z[P.size_prim:]),
+                                             z[P.size_prim:] - P.step * P.op(z[:P.size_prim])))) < tol
+    v = golden(case, "test_dotVector_d.bt")
+    ref = golden(case, "test_dotResult_d.bt")[0]
+    assert abs(c.dotM(v, v) - ref) <= (1e-9 if precision == 64 else 1e-5) * abs(ref)
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("precision,tol", [(64, 1e-10), (32, 1e-4)])
+def test_cp_step(oracle_lib, case, precision, tol):
+    """One Chambolle-Pock step T(z) (cache.cuh:795-801) from random iterates."""
+    path = os.path.join(GOLDEN, case)
+    t, d, c = make(path, precision)
+    P = oracle_lib.Problem(path)
+    x0 = x0_of(case, P.nx)
+    rng = np.random.default_rng(11)
+    for _ in range(3):
+        z = 3 * rng.standard_normal(P.size)
+        assert rel(c.cpStep(x0, z), P.cp_step(x0 * P.scaling[:P.nx], z)) < tol
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_cp_solve_fp64(oracle_lib, case):
+    """runCp: deterministic, so the GPU and the oracle take the same iterations."""
+    path = os.path.join(GOLDEN, case)
+    t, d, c = make(path, 64, tol=1e-3, max_iters=3000)
+    P = oracle_lib.Problem(path)
+    x0 = x0_of(case, P.nx)
+    st = c.runCp(x0)
+    z, s = P.run(x0, oracle_lib.options(tol=1e-3, max_iters=3000), "cp")
+    assert st == s.status
+    assert c.solveIter() == s.iters
+    assert rel(c.solution(), z) < 1e-8
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_spock_solve_fp64(oracle_lib, case):
+    """runSpock to tol 1e-3 (testCache.cu:294-308) in FP64: converged, same solution as the
+    oracle's SuperMann run."""
+    path = os.path.join(GOLDEN, case)
+    t, d, c = make(path, 64, tol=1e-3, max_iters=3000)
+    P = oracle_lib.Problem(path)
+    x0 = x0_of(case, P.nx)
+    assert c.runSpock(x0) == 0
+    z, s = P.run(x0, oracle_lib.options(tol=1e-3, max_iters=3000), "spock")
+    assert s.status == 0
+    assert abs(c.solveIter() - s.iters) <= 50
+    if c.solveIter() == s.iters:
+        assert rel(c.solution(), z) < 1e-6
+    u, xs = c.inputs(), c.states()
+    u_ref, _ = P.states_inputs(z)[1], None
+    assert np.abs(u[:P.nu] - u_ref[:P.nu]).max() < 5e-3 * max(1., np.abs(u_ref).max())
+
+
+def test_tight_solve_matches_oracle(oracle_lib):
+    """Reference test problem solved to 1e-10 (both converge): first-stage input and optimal
+    value s_0 agree to 1e-8 (FP64) and the FP32 path agrees to 1e-4."""
+    path = os.path.join(GOLDEN, "reftest")
+    P = oracle_lib.Problem(path)
+    x0 = np.full(P.nx, 1.1)
+    z, s = P.run(x0, oracle_lib.options(tol=1e-10, max_iters=20000), "spock")
+    assert s.status == 0
+    s0 = P.size_prim - P.n
+    for prec, tol, eps in [(64, 1e-8, 1e-10), (32, 1e-4, 1e-6)]:
+        t, d, c = make(path, prec, tol=eps, max_iters=20000)
+        st = c.runSpock(x0)
+        assert st == 0 or prec == 32
+        zg = c.solution()
+        assert abs(zg[s0] - z[s0]) <= tol * abs(z[s0])
+        assert np.abs(c.inputs()[:P.nu] - P.states_inputs(z)[1][:P.nu]).max() <= tol * 10
+
+
+def test_batched_fp32_matches_single(oracle_lib):
+    """A batch of 24 cfg1 instances with distinct initial states: every instance converges and
+    its first input matches the oracle's FP64 single solve."""
+    path = os.path.join(GOLDEN, "cfg1")
+    P = oracle_lib.Problem(path)
+    rng = np.random.default_rng(3)
+    x0s = rng.uniform(-1, 1, (24, P.nx))
+    t, d, c = make(path, 32, batch=24, tol=1e-3, max_iters=3000)
+    st = c.runSpockBatch(x0s)
+    assert (st == 0).all()
+    u0 = c.firstInputs()
+    for b in range(24):
+        z, s = P.run(x0s[b], oracle_lib.options(tol=1e-3, max_iters=3000), "spock")
+        u_ref = P.states_inputs(z)[1][:P.nu]
+        assert np.abs(u0[b] - u_ref).max() <= 2e-2 * max(1., np.abs(u_ref).max()), b
+
+
+def test_batch_rows_reused_cyclically(oracle_lib):
+    path = os.path.join(GOLDEN, "cfg1")
+    t, d, c = make(path, 64, batch=4, tol=1e-3, max_iters=1000)
+    x0 = golden("cfg1", "initialState_d.bt")
+    st = c.runSpockBatch(x0[None, :])
+    assert (st == 0).all()
+    u0 = c.firstInputs()
+    assert np.allclose(u0, u0[0][None, :], atol=1e-12)
+
+
+def test_warm_start_from_solution(oracle_lib):
+    """A warm start at the solution (the previousSolution path, cache.cuh:611-632) stops at
+    the first error check after the tolerance capture."""
+    path = os.path.join(GOLDEN, "cfg1")
+    t, d, c = make(path, 64, tol=1e-3, max_iters=3000)
+    x0 = golden("cfg1", "initialState_d.bt")
+    assert c.runSpock(x0) == 0
+    it_cold = c.solveIter()
+    z = c.solution()
+    assert c.runSpock(x0, prev=z) == 0
+    assert c.solveIter() <= it_cold
+
+
+def test_unsupported_types_fail_loudly():
+    path = os.path.join(GOLDEN, "affpoly")
+    t = sg.ScenarioTree(path)
+    d = sg.ProblemData(t)
+    with pytest.raises(ValueError, match="not supported"):
+        sg.CacheBuilder(t, d).build()
+
+
+def test_full_size_operator_parity(oracle_lib, tmp_problems):
+    """Config-2 sized problem (607 nodes, nx=50, nu=20): FP64 L, L*, T and M against the
+    oracle, and the adjoint identity in FP32."""
+    from spock_gb300 import configs
+    path, x0 = configs.cached("config2", tmp_problems, seed=0, count=1)
+    P = oracle_lib.Problem(path)
+    t, d, c = make(path, 64)
+    rng = np.random.default_rng(2)
+    p = rng.standard_normal(P.size_prim)
+    q = rng.standard_normal(P.size_dual)
+    assert rel(c.op(p), P.op(p)) < 1e-12
+    assert rel(c.adj(q), P.adj(q)) < 1e-12
+    z = rng.standard_normal(P.size)
+    assert rel(c.cpStep(x0[0], z), P.cp_step(x0[0] * P.scaling[:P.nx], z)) < 1e-10
+    t32, d32, c32 = make(path, 32)
+    lhs, rhs = q @ c32.op(p), c32.adj(q) @ p
+    assert abs(lhs - rhs) <= 1e-4 * max(abs(lhs), 1.)
+
+
+def test_full_size_dynamics_feasible(oracle_lib, tmp_problems):
+    """After one FP32 CP step on a config-2 problem the candidate (x, u) satisfies the
+    dynamics x_j = A_j x_anc(j) + B_j u_anc(j) and x_0 = x0 (the projection's defining
+    property, dynamics.cuh:74-174)."""
+    from spock_gb300 import configs
+    from spock_gb300.factory import read_bt
+    path, x0 = configs.cached("config2", tmp_problems, seed=0, count=1)
+    P = oracle_lib.Problem(path)
+    t, d, c = make(path, 32)
+    z = np.random.default_rng(4).standard_normal(P.size)
+    cand = c.cpStep(x0[0], z)
+    nx, nu, n, nnl = P.nx, P.nu, P.n, P.nnl
+    u = cand[:nu * nnl].reshape(nnl, nu)
+    x = cand[nu * nnl:nu * nnl + nx * n].reshape(n, nx)
+    AB = read_bt(path + "dynamics_AB_d.bt")
+    anc = read_bt(path + "ancestors_u.bt").ravel().astype(np.int64)
+    assert np.allclose(x[0], x0[0] * P.scaling[:nx], atol=1e-6)
+    pred = np.einsum("rcn,nc->nr", AB[:, :, 1:], np.concatenate((x[anc[1:]], u[anc[1:]]), axis=1))
+    assert np.abs(pred - x[1:]).max() <= 1e-4 * max(1., np.abs(x).max())
