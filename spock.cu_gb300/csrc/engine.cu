@@ -22,6 +22,7 @@
 
 #include "engine.cuh"
 #include "kernels.cuh"
+#include "kernels_batch.cuh"
 
 namespace spock {
 
@@ -34,7 +35,7 @@ namespace spock {
     } while (0)
 
 constexpr int kMaxAnderson = 8;
-constexpr int kNV0 = 5;  // r.Mr, max|Mr|, Mr.d, c.c, c.r ; then c.R_s and R_s.r per slot
+constexpr int kNV0 = 5;  // r.Mr, max|Mr|, Mr.d, c.c, c.r ; then c.R_s (8 slots) and R_s.r (8 slots)
 
 enum Action { kActNone = 0, kActFinish = 1, kActAK0 = 2, kActALs = 3, kActBK1 = 4, kActBK2 = 5, kActBK3 = 6, kActBBt = 7,
               kActCp = 8 };
@@ -62,14 +63,18 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce(const Dims Dm, const Red
     const int chunk = blockIdx.y;
     const long k0 = (long)chunk * A.rowsPerChunk;
     const long k1 = k0 + A.rowsPerChunk < Dm.sZ ? k0 + A.rowsPerChunk : Dm.sZ;
+    // accumulators indexed only by compile-time constants so they stay in registers
     T acc[kNV0 + 2 * kMaxAnderson];
-    for (int v = 0; v < A.nv; v++) acc[v] = 0;
+#pragma unroll
+    for (int v = 0; v < kNV0 + 2 * kMaxAnderson; v++) acc[v] = 0;
     T amax = 0;
     const int ph = act ? A.phase[b] : 1;
     const bool running = act && A.status[b] == -1;
     const bool wantA = running && A.algo == kSpock && ph == 0;
     const bool wantB = running && A.algo == kSpock && ph == 1;
+    const size_t slot = (size_t)Dm.sZ * B;
     if (running) {
+#pragma unroll 2
         for (long k = k0 + lane; k < k1; k += lanes) {
             const size_t o = ix(k, B, b);
             const T r = A.R[o], mr = A.MR[o];
@@ -80,17 +85,21 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce(const Dims Dm, const Red
                 const T c = r - A.RPREV[o];
                 acc[3] += c * c;
                 acc[4] += c * r;
-                for (int s = 0; s < A.m; s++) {
-                    const T a = A.ANDR[(size_t)s * Dm.sZ * B + o];
-                    acc[kNV0 + s] += c * a;
-                    acc[kNV0 + A.m + s] += a * r;
+#pragma unroll
+                for (int s = 0; s < kMaxAnderson; s++) {
+                    if (s < A.m) {
+                        const T a = A.ANDR[s * slot + o];
+                        acc[kNV0 + s] += c * a;
+                        acc[kNV0 + kMaxAnderson + s] += a * r;
+                    }
                 }
             }
         }
     }
     acc[1] = amax;
     if (laneOk)
-        for (int v = 0; v < A.nv; v++) sred[(v * lanes + lane) * TB + lb] = (double)acc[v];
+#pragma unroll
+        for (int v = 0; v < kNV0 + 2 * kMaxAnderson; v++) sred[(v * lanes + lane) * TB + lb] = (double)acc[v];
     __syncthreads();
     if (act && lane == 0)
         for (int v = 0; v < A.nv; v++) {
@@ -210,7 +219,7 @@ __global__ void k_control(const int B, const CtlArgs A) {
         for (int s = 0; s < m; s++) {
             if (s == h) continue;
             G[h * m + s] = G[s * m + h] = v[kNV0 + s];
-            rhs[s] = v[kNV0 + m + s];
+            rhs[s] = v[kNV0 + kMaxAnderson + s];
         }
         G[h * m + h] = v[3];
         rhs[h] = v[4];
@@ -358,6 +367,17 @@ __global__ void k_init_state(DevState S, int B, int warm) {
     if (b == 0) { *S.timeUp = 0; }
 }
 
+// Measurement helper: put every instance in phase A with an Anderson update pending.
+__global__ void k_force_phaseA(DevState S, int B, int m) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    S.status[b] = -1;
+    S.phase[b] = 0;
+    S.action[b] = kActALs;
+    S.useAnd[b] = 1;
+    S.head[b] = 1 % m;
+}
+
 __global__ void k_count_active(const int *status, int B, int *out) {
     __shared__ int cnt;
     if (threadIdx.x == 0) cnt = 0;
@@ -390,6 +410,7 @@ public:
         buildDims();
         upload();
         allocate();
+        chooseKernels();
         raiseSharedLimits();
     }
 
@@ -557,9 +578,8 @@ public:
     }
 
     void applyM(const double *z, double *mz) override {
-        // M z through the residual kernels with CAND = 0, so r = z
-        uploadSlice(Z_, z, 0, D_.sZ);
-        fill(CAND_, (size_t)D_.sZ * B_, T(0));
+        // M z through the residual kernels, which read the residual buffer
+        uploadSlice(R_, z, 0, D_.sZ);
         applyMres();
         downloadSlice(MR_, mz, 0, D_.sZ);
     }
@@ -569,6 +589,10 @@ public:
         CK(cudaEventCreate(&e0));
         CK(cudaEventCreate(&e1));
         std::string w(which);
+        if (w == "reduce" || w == "update") {  // time the bookkeeping with every instance in phase A
+            k_force_phaseA<<<((int)B_ + 127) / 128, 128, 0, stream_>>>(S_, (int)B_, (int)opt_.anderson);
+            CK(cudaGetLastError());
+        }
         auto once = [&]() {
             if (w == "lop") launchLop<0>(tevalLopArgs());
             else if (w == "lstar") launchLstar<0>(tevalLstarArgs());
@@ -635,6 +659,8 @@ private:
     Options opt_;
     Dims D_{};
     DevProblem<T> P_{};
+    PadMats<T> M_{};
+    bool batched_ = false;  // kernels_batch.cuh for >= 32 instances, kernels.cuh otherwise
     DevState S_{};
     cudaStream_t stream_ = nullptr;
     cudaGraphExec_t graph_ = nullptr;
@@ -714,6 +740,59 @@ private:
         scal_ = const_cast<T *>(upvec<T>(p.scaling));
     }
 
+    // Column-major matrices re-laid with the leading dimension padded to a multiple of 16 rows
+    // (zero pad), optionally transposed, for the warp-uniform vector loads of kernels_batch.cuh.
+    const T *padUpload(const std::vector<double> &src, int rows, int cols, long mats, bool transpose = false) {
+        if (src.empty()) return nullptr;
+        const int ld = pad16(rows);
+        std::vector<T> h((size_t)ld * cols * mats, T(0));
+        for (long m = 0; m < mats; m++)
+            for (int c = 0; c < cols; c++)
+                for (int r = 0; r < rows; r++) {
+                    const size_t s = transpose ? (size_t)m * rows * cols + (size_t)r * cols + c
+                                               : (size_t)m * rows * cols + (size_t)c * rows + r;
+                    h[(size_t)m * ld * cols + (size_t)c * ld + r] = (T)src[s];
+                }
+        T *d = dalloc<T>(h.size());
+        CK(cudaMemcpy(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+        return d;
+    }
+
+    // Shared memory of the batched kernels (rows staged x 32 instances).
+    size_t bLstar() const {
+        const size_t in = (size_t)std::max(D_.ne * D_.dIV + D_.nxu + D_.yD + 1 + 2 * D_.ne, D_.dVI + D_.nx);
+        const size_t base = (size_t)std::max(D_.nxu + D_.yD + 2 * D_.ne + 2, D_.nx);
+        return (in + base) * kTileB * sizeof(T);
+    }
+    size_t bLop() const {
+        const size_t in = (size_t)std::max(2 * D_.nxu + D_.yD + 2, D_.nxu + D_.nx + 2);
+        const size_t base = (size_t)std::max(D_.yD + 1 + D_.nxu + D_.dIV, D_.dIV + D_.nx + D_.dVI);
+        return ((size_t)std::max(D_.dIV, D_.dVI) + 2 * in + base) * kTileB * sizeof(T);
+    }
+    size_t bBack() const { return (size_t)(D_.ne * D_.nx + 2 * D_.nu + D_.nx) * kTileB * sizeof(T); }
+    size_t bFwd() const { return (size_t)(D_.nxu + 2 * D_.nu + D_.ne * D_.nx + D_.nx) * kTileB * sizeof(T); }
+
+    void chooseKernels() {
+        const int maxRows = kRT * kTileWarps * kMaxTasks;
+        batched_ = B_ >= kTileB && pad16(D_.nx) <= maxRows && pad16(D_.nu) <= maxRows && D_.nd <= 64 &&
+                   std::max({bLstar(), bLop(), bBack(), bFwd()}) <= 220 * 1024;
+        if (!batched_) return;
+        const HostProblem &p = hp_;
+        const int nx = D_.nx, nu = D_.nu;
+        M_.sqrtQ = padUpload(p.sqrtQ, nx, nx, p.numNodes);
+        M_.sqrtR = padUpload(p.sqrtR, nu, nu, p.numNodes);
+        M_.q = padUpload(p.q, nx, 1, p.numNodes);
+        M_.r = padUpload(p.r, nu, 1, p.numNodes);
+        M_.lSqrtQ = padUpload(p.leafSqrtQ, nx, nx, 1);
+        M_.lq = padUpload(p.leafQ, nx, 1, 1);
+        M_.BTr = padUpload(p.BTr, nu, nx, p.numNodes);
+        M_.APB = padUpload(p.APB, nx, nu, p.numNodes);
+        M_.ABKTr = padUpload(p.ABKTr, nx, nx, p.numNodes);
+        M_.Kt = padUpload(p.K, nx, nu, p.numNonleaf, true);  // K' from K (nu x nx)
+        M_.K = padUpload(p.K, nu, nx, p.numNonleaf);
+        M_.AB = padUpload(p.AB, nx, nx + nu, p.numNodes);
+    }
+
     void allocate() {
         const size_t nz = (size_t)D_.sZ * B_;
         Z_ = dalloc<T>(nz); CAND_ = dalloc<T>(nz); R_ = dalloc<T>(nz); MR_ = dalloc<T>(nz);
@@ -724,7 +803,7 @@ private:
         W1_ = dalloc<T>(nz); W2_ = dalloc<T>(nz);
         fill(Z_, nz, T(0)); fill(CAND_, nz, T(0)); fill(R_, nz, T(0)); fill(MR_, nz, T(0));
         fill(DIR_, nz, T(0)); fill(W1_, nz, T(0)); fill(W2_, nz, T(0)); fill(x0s_, (size_t)D_.nx * B_, T(0));
-        nv_ = kNV0 + 2 * (int)opt_.anderson;
+        nv_ = kNV0 + 2 * kMaxAnderson;
         const int tiles = (int)((B_ + 31) / 32);
         const int target = 1216;  // ~8 CTAs per SM
         chunks_ = std::max(1, std::min<int>(target / tiles, (int)((D_.sZ + 255) / 256)));
@@ -755,12 +834,23 @@ private:
     // Opt in to more than 48 KB of dynamic shared memory where a problem needs it.
     template <typename K>
     void optIn(K kernel, size_t bytes) {
-        if (bytes <= 48 * 1024) return;
+        if (bytes <= 40 * 1024) return;  // the default limit also covers static shared memory
         if (bytes > 227 * 1024) throw std::invalid_argument("[Cache] problem too large for the shared-memory tiles");
         CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     }
 
     void raiseSharedLimits() {
+        if (batched_) {
+            optIn(k_lstar_b<T, 0>, bLstar());
+            optIn(k_lstar_b<T, 1>, bLstar());
+            optIn(k_lstar_b<T, 2>, bLstar());
+            optIn(k_lop_b<T, 0>, bLop());
+            optIn(k_lop_b<T, 1>, bLop());
+            optIn(k_lop_b<T, 2>, bLop());
+            optIn(k_dyn_back_b<T>, bBack());
+            optIn(k_dyn_fwd_b<T>, bFwd());
+            return;
+        }
         optIn(k_dyn_back<T>, smBack());
         optIn(k_dyn_fwd<T>, smFwd());
         optIn(k_lstar<T, 0>, smLstar());
@@ -810,20 +900,20 @@ private:
         return A;
     }
 
+    // T evaluation: CAND = T(Z), and the residual R = Z - CAND of every entry as it is finalized
     OpArgs<T> tevalLstarArgs() const {  // p - gamma L* d, then prox (cache.cuh:748-764)
         OpArgs<T> A = blankArgs();
-        A.in1 = Z_; A.base1 = Z_; A.cL = -P_.step; A.out = CAND_;
+        A.in1 = Z_; A.base1 = Z_; A.cL = -P_.step; A.out = CAND_; A.outR = R_;
         return A;
     }
     OpArgs<T> tevalLopArgs() const {  // d + gamma L(2 pbar - p), then dual prox (cache.cuh:770-789)
         OpArgs<T> A = blankArgs();
-        A.in1 = CAND_; A.a1 = 2; A.in2 = Z_; A.a2 = -1; A.base1 = Z_; A.cL = P_.step; A.out = CAND_;
+        A.in1 = CAND_; A.a1 = 2; A.in2 = Z_; A.a2 = -1; A.base1 = Z_; A.cL = P_.step; A.out = CAND_; A.outR = R_;
         return A;
     }
-    OpArgs<T> mLstarArgs() const {  // r_p - gamma L* r_d, r = Z - CAND
+    OpArgs<T> mLstarArgs() const {  // M r = r - gamma [L* r_d; L r_p], reading the residual R
         OpArgs<T> A = blankArgs();
-        A.in1 = Z_; A.in2 = CAND_; A.a2 = -1; A.base1 = Z_; A.base2 = CAND_; A.b2 = -1; A.cL = -P_.step;
-        A.out = MR_; A.outBase = R_;
+        A.in1 = R_; A.base1 = R_; A.cL = -P_.step; A.out = MR_;
         return A;
     }
     OpArgs<T> mLopArgs() const {  // r_d - gamma L r_p
@@ -833,27 +923,53 @@ private:
 
     dim3 nodeGrid(int nodes) const { return dim3((unsigned)((B_ + D_.TB - 1) / D_.TB), (unsigned)nodes); }
 
+    dim3 tileGrid(int nodes) const { return dim3((unsigned)((B_ + kTileB - 1) / kTileB), (unsigned)nodes); }
+
     template <int MODE>
     void launchLstar(const OpArgs<T> &A) {
+        if (batched_) {
+            k_lstar_b<T, MODE><<<tileGrid(D_.n), kTileB * kTileWarps, bLstar(), stream_>>>(P_, D_, A, M_);
+            CK(cudaGetLastError());
+            return;
+        }
         k_lstar<T, MODE><<<nodeGrid(D_.n), kNodeThreads, smLstar(), stream_>>>(P_, D_, A);
         CK(cudaGetLastError());
     }
 
     template <int MODE>
     void launchLop(const OpArgs<T> &A) {
+        if (batched_) {
+            k_lop_b<T, MODE><<<tileGrid(D_.n), kTileB * kTileWarps, bLop(), stream_>>>(P_, D_, A, M_);
+            CK(cudaGetLastError());
+            return;
+        }
         k_lop<T, MODE><<<nodeGrid(D_.n), kNodeThreads, smLop(), stream_>>>(P_, D_, A);
         CK(cudaGetLastError());
     }
 
     void dynamics() {
         const int N = D_.ns - 1;
+        if (batched_) {
+            for (int st = N - 1; st >= 0; st--) {
+                k_dyn_back_b<T><<<tileGrid(stageCount_[st]), kTileB * kTileWarps, bBack(), stream_>>>(P_, D_, M_, CAND_, Q_, DD_,
+                                                                                                    stageFrom_[st], st);
+                CK(cudaGetLastError());
+            }
+            for (int st = 0; st < N; st++) {
+                k_dyn_fwd_b<T><<<tileGrid(stageCount_[st]), kTileB * kTileWarps, bFwd(), stream_>>>(P_, D_, M_, CAND_, DD_, x0s_,
+                                                                                                   stageFrom_[st], Z_, R_);
+                CK(cudaGetLastError());
+            }
+            return;
+        }
         const size_t smB = smBack(), smF = smFwd();
         for (int st = N - 1; st >= 0; st--) {
             k_dyn_back<T><<<nodeGrid(stageCount_[st]), kNodeThreads, smB, stream_>>>(P_, D_, CAND_, Q_, DD_, stageFrom_[st], st);
             CK(cudaGetLastError());
         }
         for (int st = 0; st < N; st++) {
-            k_dyn_fwd<T><<<nodeGrid(stageCount_[st]), kNodeThreads, smF, stream_>>>(P_, D_, CAND_, DD_, x0s_, stageFrom_[st]);
+            k_dyn_fwd<T><<<nodeGrid(stageCount_[st]), kNodeThreads, smF, stream_>>>(P_, D_, CAND_, DD_, x0s_, stageFrom_[st],
+                                                                                    Z_, R_);
             CK(cudaGetLastError());
         }
     }

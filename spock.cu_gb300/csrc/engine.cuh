@@ -53,7 +53,8 @@ struct OpArgs {
     T b1, b2;
     T cL;
     T *out;
-    T *outBase;     // when set, base is stored here too (the residual r)
+    T *outBase;     // when set, base is stored here too
+    T *outR;        // mode 0: the residual Z - out of every entry finalized by this kernel
     const T *x0s;   // scaled initial states, nx x B
 };
 

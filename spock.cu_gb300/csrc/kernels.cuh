@@ -117,6 +117,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_lstar(const DevProblem<T> P, c
                     T acc = 0;
                     for (int c = 0; c < D.nd; c++) acc += N[(size_t)c * D.nd + k] * sv[c * TB + lb];
                     A.out[ix(outk, B, b)] = acc;
+                    if (A.outR) A.outR[ix(outk, B, b)] = BASE(outk) - acc;
                 }
             }
         } else if (act) {
@@ -140,8 +141,14 @@ __global__ void __launch_bounds__(kNodeThreads) k_lstar(const DevProblem<T> P, c
     if (i == 0 && act && rg == 0) {
         EMIT(D.oT, T(0));  // t_0 carries no cost term
         const T lv = IN(D.oII);
-        if (MODE == 0) A.out[ix(D.oS, B, b)] = BASE(D.oS) + A.cL * lv - P.step;  // prox of s_0 (cache.cuh:638-642)
-        else EMIT(D.oS, lv);
+        if (MODE == 0) {
+            const T s0 = BASE(D.oS) + A.cL * lv - P.step;  // prox of s_0 (cache.cuh:638-642)
+            A.out[ix(D.oS, B, b)] = s0;
+            if (A.outR) {
+                A.outR[ix(D.oS, B, b)] = BASE(D.oS) - s0;
+                A.outR[ix(D.oT, B, b)] = T(0);
+            }
+        } else EMIT(D.oS, lv);
     }
 }
 
@@ -225,7 +232,8 @@ __global__ void __launch_bounds__(kNodeThreads) k_dyn_back(const DevProblem<T> P
 // ------------------------------------------------------------------------------------------
 template <typename T>
 __global__ void __launch_bounds__(kNodeThreads) k_dyn_fwd(const DevProblem<T> P, const Dims D, T *__restrict__ cand,
-                                                         const T *__restrict__ DD, const T *__restrict__ x0s, int stageFrom) {
+                                                         const T *__restrict__ DD, const T *__restrict__ x0s, int stageFrom,
+                                                         const T *__restrict__ Z, T *__restrict__ R) {
     extern __shared__ __align__(16) unsigned char smraw[];
     T *sx = reinterpret_cast<T *>(smraw);  // [nx][TB]
     const int TB = D.TB, B = D.B;
@@ -242,6 +250,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_dyn_fwd(const DevProblem<T> P,
             if (i == 0) {
                 v = x0s[ix(c, B, b)];
                 cand[ix(D.oX + c, B, b)] = v;
+                if (R) R[ix(D.oX + c, B, b)] = Z[ix(D.oX + c, B, b)] - v;
             } else {
                 v = cand[ix(D.oX + (long)i * nx + c, B, b)];
             }
@@ -255,6 +264,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_dyn_fwd(const DevProblem<T> P,
             for (int c = 0; c < nx; c++) acc += M[(size_t)c * nu] * sx[c * TB + lb];
             su[r * TB + lb] = acc;
             cand[ix((long)i * nu + r, B, b)] = acc;
+            if (R) R[ix((long)i * nu + r, B, b)] = Z[ix((long)i * nu + r, B, b)] - acc;
         }
     __syncthreads();
     if (!act) return;
@@ -266,6 +276,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_dyn_fwd(const DevProblem<T> P,
         for (int c = 0; c < nx; c++) acc += M[(size_t)c * nx] * sx[c * TB + lb];
         for (int c = 0; c < nu; c++) acc += M[(size_t)(nx + c) * nx] * su[c * TB + lb];
         cand[ix(D.oX + (long)j * nx + r, B, b)] = acc;
+        if (R) R[ix(D.oX + (long)j * nx + r, B, b)] = Z[ix(D.oX + (long)j * nx + r, B, b)] - acc;
     }
 }
 
@@ -313,6 +324,10 @@ __global__ void __launch_bounds__(kNodeThreads) k_lop(const DevProblem<T> P, con
         A.out[ix(k, B, b)] = bs + A.cL * lv;
     };
     // MODE 0: v = (d + gamma L.)/gamma (+ translation); cand = gamma (v - proj_C(v))  (cache.cuh:782-789)
+    auto FIN = [&](long k, T val) {
+        A.out[ix(k, B, b)] = val;
+        if (A.outR) A.outR[ix(k, B, b)] = BASE(k) - val;
+    };
 
     if (j < D.nnl) {
         if (act) {
@@ -323,7 +338,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_lop(const DevProblem<T> P, con
                 if (MODE == 0) {
                     const T v = (BASE(o) + A.cL * lv) * gi;
                     const T pr = (k < nm && v < T(0)) ? T(0) * v : v;  // AVaR dual cone (risks.cuh:99-106)
-                    A.out[ix(o, B, b)] = (v - pr) * g;
+                    FIN(o, (v - pr) * g);
                 } else EMIT(o, lv);
             }
             if (rg == 0) {
@@ -332,7 +347,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_lop(const DevProblem<T> P, con
                 const long o = D.oII + j;
                 if (MODE == 0) {
                     const T v = (BASE(o) + A.cL * lv) * gi;
-                    A.out[ix(o, B, b)] = (v - (v > T(0) ? v : T(0))) * g;  // nonnegative orthant
+                    FIN(o, (v - (v > T(0) ? v : T(0))) * g);  // nonnegative orthant
                 } else EMIT(o, lv);
             }
             if (D.conNl == kConRectangle)
@@ -342,7 +357,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_lop(const DevProblem<T> P, con
                     if (MODE == 0) {
                         const T v = (BASE(o) + A.cL * lv) * gi;
                         const T pr = boxProject(v, P.nlLo[(size_t)j * nxu + k], P.nlHi[(size_t)j * nxu + k]);
-                        A.out[ix(o, B, b)] = (v - pr) * g;
+                        FIN(o, (v - pr) * g);
                     } else EMIT(o, lv);
                 }
         }
@@ -396,7 +411,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_lop(const DevProblem<T> P, con
                     const T v = sw[c * TB + lb];
                     const int cs = sCase[lb];
                     const T pr = cs == 1 ? v : (cs == 2 ? T(0) : (c < dIV - 1 ? sScale[lb] * v : sScale[lb] * sNrm[lb]));
-                    A.out[ix(ivo + c, B, b)] = (v - pr) * g;
+                    FIN(ivo + c, (v - pr) * g);
                 }
         } else if (act) {
             for (int c = rg; c < dIV; c += RG) EMIT(ivo + c, lvIV(c));
@@ -411,7 +426,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_lop(const DevProblem<T> P, con
                 if (MODE == 0) {
                     const T v = (BASE(o) + A.cL * lv) * gi;
                     const T pr = boxProject(v, P.lLo[(size_t)l * nx + k], P.lHi[(size_t)l * nx + k]);
-                    A.out[ix(o, B, b)] = (v - pr) * g;
+                    FIN(o, (v - pr) * g);
                 } else EMIT(o, lv);
             }
         const int dVI = D.dVI;
@@ -451,7 +466,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_lop(const DevProblem<T> P, con
                     const T v = sw[c * TB + lb];
                     const int cs = sCase[lb];
                     const T pr = cs == 1 ? v : (cs == 2 ? T(0) : (c < dVI - 1 ? sScale[lb] * v : sScale[lb] * sNrm[lb]));
-                    A.out[ix(vio + c, B, b)] = (v - pr) * g;
+                    FIN(vio + c, (v - pr) * g);
                 }
         } else if (act) {
             for (int c = rg; c < dVI; c += RG) EMIT(vio + c, lvVI(c));

@@ -1,0 +1,683 @@
+// Node kernels for batches of >= 32 instances (sm_103a, FP32 or FP64).
+//
+// Same mathematics as kernels.cuh (which serves small batches and the single-instance solve),
+// mapped for throughput.  A CTA owns one tree node and a tile of 32 instances, one per lane:
+//  1. gather: every input row and every base row the CTA needs (for a row k, the 32
+//     instances k*B + b0 .. b0+31 are one 128-byte coalesced segment) is copied into shared
+//     memory with cp.async, all issued before the first wait, so hundreds of loads are in
+//     flight per SM;
+//  2. compute: each warp accumulates blocks of 16 output rows in registers (16 FMAs per
+//     shared-memory input read); matrix columns are read as warp-uniform 16-byte loads from
+//     device copies whose leading dimension is padded to a multiple of 16 (L1/L2 resident,
+//     shared by all tiles of the node);
+//  3. write: outputs (and, in a T evaluation, the residual Z - T(Z)) go out as coalesced rows.
+// Nothing in steps 2-3 reads global memory through a pointer that a store could alias.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace spock {
+
+constexpr int kTileB = 32;     // instances per CTA (one per lane)
+constexpr int kTileWarps = 4;  // warps per CTA
+constexpr int kRT = 16;        // output rows per register block
+constexpr int kMaxTasks = 2;   // register blocks per warp: rows <= 16 * 4 * 2 = 128
+
+__host__ __device__ inline int pad16(int r) { return (r + 15) & ~15; }
+
+// Pre-padded per-node matrices (column-major, leading dimension pad16(rows)).
+template <typename T>
+struct PadMats {
+    const T *sqrtQ, *sqrtR, *q, *r;  // nonleaf cost, per node
+    const T *lSqrtQ, *lq;            // leaf cost
+    const T *BTr, *APB, *ABKTr;      // per node (child j)
+    const T *Kt, *K;                 // per nonleaf node: K' (nx x nu), K (nu x nx)
+    const T *AB;                     // per node: [A B] (nx x nxu)
+};
+
+__device__ __forceinline__ unsigned smemAddr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+template <typename T>
+__device__ __forceinline__ void cpAsyncElem(T *dst, const T *src) {
+    if (sizeof(T) == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smemAddr(dst)), "l"(src));
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smemAddr(dst)), "l"(src));
+}
+
+__device__ __forceinline__ void cpAsyncWaitAll() {
+    asm volatile("cp.async.commit_group;\n" ::);
+    asm volatile("cp.async.wait_group 0;\n" ::);
+}
+
+// 16 consecutive matrix entries (16-byte aligned) as warp-uniform vector loads.
+__device__ __forceinline__ void load16(const float *p, float v[kRT]) {
+    const float4 *q = reinterpret_cast<const float4 *>(p);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const float4 a = __ldg(q + i);
+        v[4 * i] = a.x; v[4 * i + 1] = a.y; v[4 * i + 2] = a.z; v[4 * i + 3] = a.w;
+    }
+}
+
+__device__ __forceinline__ void load16(const double *p, double v[kRT]) {
+    const double2 *q = reinterpret_cast<const double2 *>(p);
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const double2 a = __ldg(q + i);
+        v[2 * i] = a.x; v[2 * i + 1] = a.y;
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void zeroAcc(T acc[kMaxTasks][kRT]) {
+#pragma unroll
+    for (int q = 0; q < kMaxTasks; q++)
+#pragma unroll
+        for (int t = 0; t < kRT; t++) acc[q][t] = T(0);
+}
+
+// acc[q][t] += sum_k M[(warp + 4q)*16 + t, k] * in(k), M padded column-major (ld = pad16(rows)).
+template <typename T, typename In>
+__device__ __forceinline__ void gemv(T acc[kMaxTasks][kRT], const T *M, int rows, int K, int warp, In in) {
+    const int ld = pad16(rows);
+    const int nTasks = ld / kRT;
+#pragma unroll
+    for (int q = 0; q < kMaxTasks; q++) {
+        const int task = warp + q * kTileWarps;
+        if (task >= nTasks) continue;
+        const T *col = M + task * kRT;
+        int k = 0;
+        for (; k + 2 <= K; k += 2) {
+            T m0[kRT], m1[kRT];
+            load16(col + (size_t)k * ld, m0);
+            load16(col + (size_t)(k + 1) * ld, m1);
+            const T v0 = in(k), v1 = in(k + 1);
+#pragma unroll
+            for (int t = 0; t < kRT; t++) acc[q][t] += m0[t] * v0;
+#pragma unroll
+            for (int t = 0; t < kRT; t++) acc[q][t] += m1[t] * v1;
+        }
+        if (k < K) {
+            T m0[kRT];
+            load16(col + (size_t)k * ld, m0);
+            const T v0 = in(k);
+#pragma unroll
+            for (int t = 0; t < kRT; t++) acc[q][t] += m0[t] * v0;
+        }
+    }
+}
+
+// Gather rows rowOf(0..n-1) of `src` for instances b0 .. b0+31 into sm[r*32 + lane].
+template <typename T, typename RowOf>
+__device__ __forceinline__ void gather(T *sm, int n, const T *src, int B, int b0, int lane, int warp, RowOf rowOf) {
+    const int bs = (b0 + lane < B) ? b0 + lane : 0;
+    for (int r = warp; r < n; r += kTileWarps) cpAsyncElem(sm + r * kTileB + lane, src + (size_t)rowOf(r) * B + bs);
+}
+
+// ------------------------------------------------------------------------------------------
+// L* (MODE 0: with the primal prox of cache.cuh:748-764; 1: M form; 2: bare)
+// input rows, nonleaf i: [IV_j, j in ch(i)][III_i][I_i][II_i][s-source of each child, 2 rows]
+//             leaf i:    [VI_l][V_l]
+// base rows,  nonleaf i: [x_i][u_i][y_i][t_ch][s_ch][t_0 s_0 at the root];  leaf: [x_i]
+// ------------------------------------------------------------------------------------------
+template <typename T, int MODE>
+__global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem<T> P, const Dims D, const OpArgs<T> A,
+                                                                const PadMats<T> M) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T *sm = reinterpret_cast<T *>(smraw);
+    const int B = D.B, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int b0 = blockIdx.x * kTileB, b = b0 + lane;
+    const bool act = b < B;
+    const int i = blockIdx.y;
+    const int nx = D.nx, nu = D.nu, nxu = D.nxu, dIV = D.dIV, dVI = D.dVI, yD = D.yD;
+    const bool nonleaf = i < D.nnl;
+    const int c0 = nonleaf ? P.chFrom[i] : 0, nc = nonleaf ? P.numCh[i] : 0;
+    const int l = i - D.nnl;
+    const bool rect = nonleaf ? D.conNl == kConRectangle : D.conL == kConRectangle;
+    // input row map
+    const int rIII = nc * dIV, rI = rIII + (rect ? nxu : 0), rII = rI + yD, rS = rII + 1;
+    const int nIn = nonleaf ? rS + 2 * nc : dVI + (rect ? nx : 0);
+    auto rowIn = [&](int r) -> long {
+        if (!nonleaf) return r < dVI ? D.oVI + (long)l * dVI + r : D.oV + (long)l * nx + (r - dVI);
+        if (r < rIII) return D.oIV + (long)(c0 + r / dIV) * dIV + r % dIV;
+        if (r < rI) return D.oIII + (long)i * nxu + (r - rIII);
+        if (r < rII) return D.oI + (long)i * yD + (r - rI);
+        if (r == rII) return D.oII + i;
+        const int jj = (r - rS) >> 1, j = c0 + jj;
+        if (j < D.nnl) return D.oII + j;
+        return D.oVI + (long)(j - D.nnl) * dVI + nx + ((r - rS) & 1);
+    };
+    const int bY = nxu, bT = bY + yD, bS = bT + nc, bRoot = bS + nc;
+    const int nBase = nonleaf ? bRoot + (i == 0 ? 2 : 0) : nx;
+    auto rowBase = [&](int r) -> long {
+        if (!nonleaf || r < nx) return D.oX + (long)i * nx + r;
+        if (r < bY) return (long)i * nu + (r - nx);
+        if (r < bT) return D.oY + (long)i * yD + (r - bY);
+        if (r < bS) return D.oT + c0 + (r - bT);
+        if (r < bRoot) return D.oS + c0 + (r - bS);
+        return r == bRoot ? D.oT : D.oS;
+    };
+    const int inArr = A.in2 ? 2 : 1, baseArr = A.base2 ? 2 : (A.base1 ? 1 : 0);
+    T *sIn = sm, *sBase = sIn + nIn * inArr * kTileB;
+    gather(sIn, nIn, A.in1, B, b0, lane, warp, rowIn);
+    if (A.in2) gather(sIn + nIn * kTileB, nIn, A.in2, B, b0, lane, warp, rowIn);
+    if (A.base1) gather(sBase, nBase, A.base1, B, b0, lane, warp, rowBase);
+    if (A.base2) gather(sBase + nBase * kTileB, nBase, A.base2, B, b0, lane, warp, rowBase);
+    cpAsyncWaitAll();
+    __syncthreads();
+    auto IN = [&](int r) -> T {
+        T v = A.a1 * sIn[r * kTileB + lane];
+        if (inArr == 2) v += A.a2 * sIn[(nIn + r) * kTileB + lane];
+        return v;
+    };
+    auto BASE = [&](int r) -> T {
+        if (!baseArr) return T(0);
+        T v = A.b1 * sBase[r * kTileB + lane];
+        if (baseArr == 2) v += A.b2 * sBase[(nBase + r) * kTileB + lane];
+        return v;
+    };
+    auto EMIT = [&](int rb, T lv) {
+        if (!act) return;
+        const T bs = BASE(rb);
+        const size_t o = (size_t)rowBase(rb) * B + b;
+        if (A.outBase) A.outBase[o] = bs;
+        A.out[o] = bs + A.cL * lv;
+    };
+    auto FIN = [&](int rb, T val) {  // a final primal entry (mode 0) and its residual
+        if (!act) return;
+        const size_t o = (size_t)rowBase(rb) * B + b;
+        A.out[o] = val;
+        if (A.outR) A.outR[o] = BASE(rb) - val;
+    };
+    T accX[kMaxTasks][kRT], accU[kMaxTasks][kRT];
+    zeroAcc(accX);
+    zeroAcc(accU);
+    if (nonleaf) {
+        const bool qpl = D.costNl == kCostQuadraticPlusLinear;
+        const int ldx = pad16(nx), ldu = pad16(nu);
+        for (int jj = 0; jj < nc; jj++) {
+            const int j = c0 + jj, r0 = jj * dIV;
+            gemv(accX, M.sqrtQ + (size_t)j * ldx * nx, nx, nx, warp, [&](int k) { return IN(r0 + k); });
+            gemv(accU, M.sqrtR + (size_t)j * ldu * nu, nu, nu, warp, [&](int k) { return IN(r0 + nx + k); });
+            if (qpl) {
+                const T d23 = T(-0.5) * (IN(r0 + nxu) + IN(r0 + nxu + 1));
+                gemv(accX, M.q + (size_t)j * ldx, nx, 1, warp, [&](int) { return d23; });
+                gemv(accU, M.r + (size_t)j * ldu, nu, 1, warp, [&](int) { return d23; });
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kMaxTasks; q++) {
+            const int r0 = (warp + q * kTileWarps) * kRT;
+#pragma unroll
+            for (int t = 0; t < kRT; t++) {
+                const int r = r0 + t;
+                if (r < nx) EMIT(r, accX[q][t] + (rect ? IN(rIII + r) : T(0)));
+                if (r < nu) EMIT(nx + r, accU[q][t] + (rect ? IN(rIII + nx + r) : T(0)));
+            }
+        }
+        // y_i, the children's t and s, and the AVaR kernel projection (cache.cuh:650-676),
+        // one lane per instance on warp 0 (the 4E+1 vector is small)
+        if (warp == 0) {
+            const T II = IN(rII);
+            T v[64];
+            int ob[64];
+            for (int k = 0; k < D.nd; k++) {
+                T lv = 0;
+                ob[k] = -1;
+                if (k < yD) {
+                    ob[k] = bY + k;
+                    lv = IN(rI + k) - P.b[(size_t)i * yD + k] * II;
+                } else if (k < yD + D.ne) {
+                    const int jj = k - yD;
+                    if (jj < nc) {
+                        ob[k] = bT + jj;
+                        lv = T(0.5) * (IN(jj * dIV + nxu) + IN(jj * dIV + nxu + 1));
+                    }
+                } else {
+                    const int jj = k - yD - D.ne;
+                    if (jj < nc) {
+                        ob[k] = bS + jj;
+                        lv = (c0 + jj < D.nnl) ? IN(rS + 2 * jj) : T(0.5) * (IN(rS + 2 * jj) + IN(rS + 2 * jj + 1));
+                    }
+                }
+                if (MODE == 0) v[k] = ob[k] >= 0 ? BASE(ob[k]) + A.cL * lv : T(0);
+                else if (ob[k] >= 0) EMIT(ob[k], lv);
+            }
+            if (MODE == 0) {
+                const T *N = P.NNtr + (size_t)i * D.nd * D.nd;
+                for (int k = 0; k < D.nd; k++) {
+                    if (ob[k] < 0) continue;
+                    T acc = 0;
+                    for (int c = 0; c < D.nd; c++) acc += __ldg(N + (size_t)c * D.nd + k) * v[c];
+                    FIN(ob[k], acc);
+                }
+            }
+            if (i == 0) {  // t_0 carries no cost term; s_0 gets the prox of the objective
+                if (MODE == 0) {
+                    FIN(bRoot, BASE(bRoot));
+                    FIN(bRoot + 1, BASE(bRoot + 1) + A.cL * II - P.step);
+                } else {
+                    EMIT(bRoot, T(0));
+                    EMIT(bRoot + 1, II);
+                }
+            }
+        }
+    } else {
+        const int ldx = pad16(nx);
+        gemv(accX, M.lSqrtQ, nx, nx, warp, [&](int k) { return IN(k); });
+        if (D.costL == kCostQuadraticPlusLinear) {
+            const T d23 = T(-0.5) * (IN(nx) + IN(nx + 1));
+            gemv(accX, M.lq, nx, 1, warp, [&](int) { return d23; });
+        }
+        (void)ldx;
+#pragma unroll
+        for (int q = 0; q < kMaxTasks; q++) {
+            const int r0 = (warp + q * kTileWarps) * kRT;
+#pragma unroll
+            for (int t = 0; t < kRT; t++) {
+                const int r = r0 + t;
+                if (r < nx) EMIT(r, accX[q][t] + (rect ? IN(dVI + r) : T(0)));
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// L (MODE 0: with the dual prox of cache.cuh:770-789; 1: M form; 2: bare)
+// input rows: [x_a][u_a][t_j] (a = ancestor of j; zero rows at the root), then nonleaf j:
+//             [y_j][s_j][x_j][u_j], leaf j: [x_j][s_j]
+// base rows:  nonleaf j: [I_j][II_j][III_j][IV_j];  leaf j: [IV_j][V_l][VI_l]
+// ------------------------------------------------------------------------------------------
+template <typename T, int MODE>
+__global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T> P, const Dims D, const OpArgs<T> A,
+                                                              const PadMats<T> M) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T *sm = reinterpret_cast<T *>(smraw);
+    const int B = D.B, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int b0 = blockIdx.x * kTileB, b = b0 + lane;
+    const bool act = b < B;
+    const int j = blockIdx.y;
+    const int nx = D.nx, nu = D.nu, nxu = D.nxu, dIV = D.dIV, dVI = D.dVI, yD = D.yD;
+    const bool nonleaf = j < D.nnl;
+    const int l = j - D.nnl;
+    const int a = j > 0 ? P.anc[j] : 0;
+    const bool rect = nonleaf ? D.conNl == kConRectangle : D.conL == kConRectangle;
+    const T g = P.step, gi = T(1) / P.step;
+    const int rOwn = nxu + 1;
+    const int nIn = nonleaf ? rOwn + yD + 1 + nxu : rOwn + nx + 1;
+    auto rowIn = [&](int r) -> long {
+        if (r < nx) return D.oX + (long)a * nx + r;
+        if (r < nxu) return (long)a * nu + (r - nx);
+        if (r == nxu) return D.oT + j;
+        const int q = r - rOwn;
+        if (nonleaf) {
+            if (q < yD) return D.oY + (long)j * yD + q;
+            if (q == yD) return D.oS + j;
+            if (q < yD + 1 + nx) return D.oX + (long)j * nx + (q - yD - 1);
+            return (long)j * nu + (q - yD - 1 - nx);
+        }
+        if (q < nx) return D.oX + (long)j * nx + q;
+        return D.oS + j;
+    };
+    const int bIII = yD + 1, bIVn = bIII + (rect ? nxu : 0);
+    const int bIV = nonleaf ? bIVn : 0, bV = dIV, bVI = dIV + (rect ? nx : 0);
+    const int nBase = nonleaf ? bIVn + dIV : bVI + dVI;
+    auto rowBase = [&](int r) -> long {
+        if (nonleaf) {
+            if (r < yD) return D.oI + (long)j * yD + r;
+            if (r == yD) return D.oII + j;
+            if (r < bIVn) return D.oIII + (long)j * nxu + (r - bIII);
+            return D.oIV + (long)j * dIV + (r - bIVn);
+        }
+        if (r < bV) return D.oIV + (long)j * dIV + r;
+        if (r < bVI) return D.oV + (long)l * nx + (r - bV);
+        return D.oVI + (long)l * dVI + (r - bVI);
+    };
+    const int inArr = A.in2 ? 2 : 1, baseArr = A.base2 ? 2 : (A.base1 ? 1 : 0);
+    const int dSoc = dIV > dVI ? dIV : dVI;
+    T *sw = sm, *sIn = sw + dSoc * kTileB, *sBase = sIn + nIn * inArr * kTileB;
+    gather(sIn, nIn, A.in1, B, b0, lane, warp, rowIn);
+    if (A.in2) gather(sIn + nIn * kTileB, nIn, A.in2, B, b0, lane, warp, rowIn);
+    if (A.base1) gather(sBase, nBase, A.base1, B, b0, lane, warp, rowBase);
+    if (A.base2) gather(sBase + nBase * kTileB, nBase, A.base2, B, b0, lane, warp, rowBase);
+    cpAsyncWaitAll();
+    __syncthreads();
+    auto INP = [&](int r) -> T {
+        T v = A.a1 * sIn[r * kTileB + lane];
+        if (inArr == 2) v += A.a2 * sIn[(nIn + r) * kTileB + lane];
+        return v;
+    };
+    auto BASE = [&](int r) -> T {
+        if (!baseArr) return T(0);
+        T v = A.b1 * sBase[r * kTileB + lane];
+        if (baseArr == 2) v += A.b2 * sBase[(nBase + r) * kTileB + lane];
+        return v;
+    };
+    auto EMIT = [&](int rb, T lv) {
+        if (!act) return;
+        const T bs = BASE(rb);
+        const size_t o = (size_t)rowBase(rb) * B + b;
+        if (A.outBase) A.outBase[o] = bs;
+        A.out[o] = bs + A.cL * lv;
+    };
+    auto FIN = [&](int rb, T val) {  // a final dual entry (mode 0) and its residual
+        if (!act) return;
+        const size_t o = (size_t)rowBase(rb) * B + b;
+        A.out[o] = val;
+        if (A.outR) A.outR[o] = BASE(rb) - val;
+    };
+    // (v - proj(v)) * gamma for an SOC block staged in sw (dim rows), warp 0 only
+    auto socBlock = [&](int dim, int rb0) {
+        if (warp != 0) return;
+        T ss = 0;
+        for (int c = 0; c < dim - 1; c++) ss += sw[c * kTileB + lane] * sw[c * kTileB + lane];
+        const T nrm = sqrt(ss), tt = sw[(dim - 1) * kTileB + lane];
+        const int i1 = nrm <= tt, i2 = (nrm <= -tt) && !i1, i3 = !i1 && !i2;
+        const T sc = (nrm + tt) / (T(2) * nrm + T(1 - i3));
+        for (int c = 0; c < dim; c++) {
+            const T v = sw[c * kTileB + lane];
+            const T pr = i1 ? v : (i2 ? T(0) : (c < dim - 1 ? sc * v : sc * nrm));
+            FIN(rb0 + c, (v - pr) * g);
+        }
+    };
+    if (nonleaf) {
+        const int nm = 2 * P.numCh[j];
+        const int ry = rOwn, rs = rOwn + yD, rx = rs + 1, ru = rx + nx;
+        for (int k = warp; k < yD; k += kTileWarps) {
+            const T lv = INP(ry + k);
+            if (MODE == 0) {
+                const T v = (BASE(k) + A.cL * lv) * gi;
+                const T pr = (k < nm && v < T(0)) ? T(0) * v : v;  // AVaR dual cone (risks.cuh:99-106)
+                FIN(k, (v - pr) * g);
+            } else EMIT(k, lv);
+        }
+        if (warp == kTileWarps - 1) {
+            T lv = INP(rs);
+            for (int k = 0; k < yD; k++) lv -= __ldg(P.b + (size_t)j * yD + k) * INP(ry + k);
+            if (MODE == 0) {
+                const T v = (BASE(yD) + A.cL * lv) * gi;
+                FIN(yD, (v - (v > T(0) ? v : T(0))) * g);
+            } else EMIT(yD, lv);
+        }
+        if (rect)
+            for (int k = warp; k < nxu; k += kTileWarps) {
+                const T lv = k < nx ? INP(rx + k) : INP(ru + k - nx);
+                if (MODE == 0) {
+                    const T v = (BASE(bIII + k) + A.cL * lv) * gi;
+                    const T pr = boxProject(v, P.nlLo[(size_t)j * nxu + k], P.nlHi[(size_t)j * nxu + k]);
+                    FIN(bIII + k, (v - pr) * g);
+                } else EMIT(bIII + k, lv);
+            }
+    }
+    {  // IV_j = [sqrtQ_j x_a; sqrtR_j u_a; h; h] (costs.cuh:126-161, 379-417); zero at the root
+        T accX[kMaxTasks][kRT], accU[kMaxTasks][kRT];
+        zeroAcc(accX);
+        zeroAcc(accU);
+        T h = 0;
+        if (j > 0) {
+            const int ldx = pad16(nx), ldu = pad16(nu);
+            gemv(accX, M.sqrtQ + (size_t)j * ldx * nx, nx, nx, warp, [&](int k) { return INP(k); });
+            gemv(accU, M.sqrtR + (size_t)j * ldu * nu, nu, nu, warp, [&](int k) { return INP(nx + k); });
+            h = T(0.5) * INP(nxu);
+            if (D.costNl == kCostQuadraticPlusLinear) {
+                T lin = 0;
+                for (int k = 0; k < nx; k++) lin += __ldg(P.q + (size_t)j * nx + k) * INP(k);
+                for (int k = 0; k < nu; k++) lin += __ldg(P.r + (size_t)j * nu + k) * INP(nx + k);
+                h -= T(0.5) * lin;
+            }
+        }
+        if (MODE == 0) {
+#pragma unroll
+            for (int q = 0; q < kMaxTasks; q++) {
+                const int r0 = (warp + q * kTileWarps) * kRT;
+#pragma unroll
+                for (int t = 0; t < kRT; t++) {
+                    const int r = r0 + t;
+                    if (r < nx) sw[r * kTileB + lane] = (BASE(bIV + r) + A.cL * accX[q][t]) * gi + P.trans[(size_t)j * dIV + r];
+                    if (r < nu)
+                        sw[(nx + r) * kTileB + lane] =
+                            (BASE(bIV + nx + r) + A.cL * accU[q][t]) * gi + P.trans[(size_t)j * dIV + nx + r];
+                }
+            }
+            if (warp == 0)
+                for (int r = nxu; r < dIV; r++) sw[r * kTileB + lane] = (BASE(bIV + r) + A.cL * h) * gi + P.trans[(size_t)j * dIV + r];
+            __syncthreads();
+            socBlock(dIV, bIV);
+        } else {
+#pragma unroll
+            for (int q = 0; q < kMaxTasks; q++) {
+                const int r0 = (warp + q * kTileWarps) * kRT;
+#pragma unroll
+                for (int t = 0; t < kRT; t++) {
+                    const int r = r0 + t;
+                    if (r < nx) EMIT(bIV + r, accX[q][t]);
+                    if (r < nu) EMIT(bIV + nx + r, accU[q][t]);
+                }
+            }
+            if (warp == 0)
+                for (int r = nxu; r < dIV; r++) EMIT(bIV + r, h);
+        }
+    }
+    if (!nonleaf) {  // V and VI of a leaf (constraints.cuh:168-170, costs.cuh:149-161/404-417)
+        const int rx = rOwn, rs = rOwn + nx;
+        if (rect)
+            for (int k = warp; k < nx; k += kTileWarps) {
+                const T lv = INP(rx + k);
+                if (MODE == 0) {
+                    const T v = (BASE(bV + k) + A.cL * lv) * gi;
+                    const T pr = boxProject(v, P.lLo[(size_t)l * nx + k], P.lHi[(size_t)l * nx + k]);
+                    FIN(bV + k, (v - pr) * g);
+                } else EMIT(bV + k, lv);
+            }
+        T accX[kMaxTasks][kRT];
+        zeroAcc(accX);
+        gemv(accX, M.lSqrtQ, nx, nx, warp, [&](int k) { return INP(rx + k); });
+        T h = T(0.5) * INP(rs);
+        if (D.costL == kCostQuadraticPlusLinear) {
+            T lin = 0;
+            for (int k = 0; k < nx; k++) lin += __ldg(P.lq + k) * INP(rx + k);
+            h -= T(0.5) * lin;
+        }
+        if (MODE == 0) {
+            __syncthreads();  // sw is reused after the IV block
+#pragma unroll
+            for (int q = 0; q < kMaxTasks; q++) {
+                const int r0 = (warp + q * kTileWarps) * kRT;
+#pragma unroll
+                for (int t = 0; t < kRT; t++) {
+                    const int r = r0 + t;
+                    if (r < nx) sw[r * kTileB + lane] = (BASE(bVI + r) + A.cL * accX[q][t]) * gi + P.lTrans[r];
+                }
+            }
+            if (warp == 0)
+                for (int r = nx; r < dVI; r++) sw[r * kTileB + lane] = (BASE(bVI + r) + A.cL * h) * gi + P.lTrans[r];
+            __syncthreads();
+            socBlock(dVI, bVI);
+        } else {
+#pragma unroll
+            for (int q = 0; q < kMaxTasks; q++) {
+                const int r0 = (warp + q * kTileWarps) * kRT;
+#pragma unroll
+                for (int t = 0; t < kRT; t++) {
+                    const int r = r0 + t;
+                    if (r < nx) EMIT(bVI + r, accX[q][t]);
+                }
+            }
+            if (warp == 0)
+                for (int r = nx; r < dVI; r++) EMIT(bVI + r, h);
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Dynamics projection, one stage of the backward sweep (dynamics.cuh:85-139).
+// inputs: q of the children (-x of leaves at the last stage, else Q), u_i, x_i
+// ------------------------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(kTileB *kTileWarps) k_dyn_back_b(const DevProblem<T> P, const Dims D, const PadMats<T> M,
+                                                                  const T *__restrict__ cand, T *__restrict__ Q,
+                                                                  T *__restrict__ DD, int stageFrom, int stage) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T *sm = reinterpret_cast<T *>(smraw);
+    const int B = D.B, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int b0 = blockIdx.x * kTileB, b = b0 + lane;
+    const bool act = b < B;
+    const int i = stageFrom + blockIdx.y;
+    const int nx = D.nx, nu = D.nu;
+    const int c0 = P.chFrom[i], nc = P.numCh[i];
+    const bool leafChildren = c0 >= D.nnl;
+    T *sq = sm, *su = sq + nc * nx * kTileB, *sx = su + nu * kTileB, *sd = sx + nx * kTileB;
+    if (leafChildren)
+        gather(sq, nc * nx, cand, B, b0, lane, warp, [&](int r) { return D.oX + (long)c0 * nx + r; });
+    else
+        gather(sq, nc * nx, (const T *)Q, B, b0, lane, warp, [&](int r) { return (long)c0 * nx + r; });
+    gather(su, nu, cand, B, b0, lane, warp, [&](int r) { return (long)i * nu + r; });
+    if (stage > 0) gather(sx, nx, cand, B, b0, lane, warp, [&](int r) { return D.oX + (long)i * nx + r; });
+    cpAsyncWaitAll();
+    __syncthreads();
+    if (leafChildren || D.affine) {  // q of a leaf is -x; affine dynamics add P e (dynamics.cuh:96-99)
+        for (int t = warp; t < nc * nx; t += kTileWarps) {
+            T v = sq[t * kTileB + lane];
+            if (leafChildren) v = -v;
+            if (D.affine) v += P.Pe[(size_t)c0 * nx + t];
+            sq[t * kTileB + lane] = v;
+        }
+        __syncthreads();
+    }
+    const int ldx = pad16(nx), ldu = pad16(nu);
+    T acc[kMaxTasks][kRT];
+    zeroAcc(acc);
+    for (int jj = 0; jj < nc; jj++) {
+        const T *qv = sq + jj * nx * kTileB + lane;
+        gemv(acc, M.BTr + (size_t)(c0 + jj) * ldu * nx, nu, nx, warp, [&](int k) { return qv[k * kTileB]; });
+    }
+#pragma unroll
+    for (int q = 0; q < kMaxTasks; q++) {
+        const int r0 = (warp + q * kTileWarps) * kRT;
+#pragma unroll
+        for (int t = 0; t < kRT; t++) {
+            const int r = r0 + t;
+            if (r < nu) sd[r * kTileB + lane] = su[r * kTileB + lane] - acc[q][t];
+        }
+    }
+    __syncthreads();
+    if (warp == 0) {  // (I + sum B'PB) d = rhs with the cached lower Cholesky factor
+        const T *L = P.chol + (size_t)i * nu * nu;
+        T *v = sd + lane;
+        for (int r = 0; r < nu; r++) {
+            T s = v[r * kTileB];
+            for (int k = 0; k < r; k++) s -= __ldg(L + (size_t)k * nu + r) * v[k * kTileB];
+            v[r * kTileB] = s / __ldg(L + (size_t)r * nu + r);
+        }
+        for (int r = nu - 1; r >= 0; r--) {
+            T s = v[r * kTileB];
+            for (int k = r + 1; k < nu; k++) s -= __ldg(L + (size_t)r * nu + k) * v[k * kTileB];
+            v[r * kTileB] = s / __ldg(L + (size_t)r * nu + r);
+        }
+    }
+    __syncthreads();
+    if (act)
+        for (int r = warp; r < nu; r += kTileWarps) DD[ix((long)i * nu + r, B, b)] = sd[r * kTileB + lane];
+    if (stage == 0) return;
+    zeroAcc(acc);
+    for (int jj = 0; jj < nc; jj++) {
+        const int j = c0 + jj;
+        const T *qv = sq + jj * nx * kTileB + lane;
+        gemv(acc, M.APB + (size_t)j * ldx * nu, nx, nu, warp, [&](int k) { return sd[k * kTileB + lane]; });
+        gemv(acc, M.ABKTr + (size_t)j * ldx * nx, nx, nx, warp, [&](int k) { return qv[k * kTileB]; });
+    }
+    gemv(acc, M.Kt + (size_t)i * ldx * nu, nx, nu, warp,
+         [&](int k) { return sd[k * kTileB + lane] - su[k * kTileB + lane]; });
+    if (!act) return;
+#pragma unroll
+    for (int q = 0; q < kMaxTasks; q++) {
+        const int r0 = (warp + q * kTileWarps) * kRT;
+#pragma unroll
+        for (int t = 0; t < kRT; t++) {
+            const int r = r0 + t;
+            if (r < nx) Q[ix((long)i * nx + r, B, b)] = acc[q][t] - sx[r * kTileB + lane];
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Dynamics projection, one stage of the forward rollout (dynamics.cuh:143-173), writing the
+// candidate (x, u) and its residual Z - cand.
+// ------------------------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(kTileB *kTileWarps) k_dyn_fwd_b(const DevProblem<T> P, const Dims D, const PadMats<T> M,
+                                                                 T *__restrict__ cand, const T *__restrict__ DD,
+                                                                 const T *__restrict__ x0s, int stageFrom,
+                                                                 const T *__restrict__ Z, T *__restrict__ R) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T *sm = reinterpret_cast<T *>(smraw);
+    const int B = D.B, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int b0 = blockIdx.x * kTileB, b = b0 + lane;
+    const bool act = b < B;
+    const int i = stageFrom + blockIdx.y;
+    const int nx = D.nx, nu = D.nu, nxu = D.nxu;
+    const int c0 = P.chFrom[i], nc = P.numCh[i];
+    T *sxu = sm, *sdd = sxu + nxu * kTileB, *sz = sdd + nu * kTileB;  // sz: Z of [u_i][x_children][x_0]
+    const int nZ = nu + nc * nx + (i == 0 ? nx : 0);
+    if (i == 0) gather(sxu, nx, x0s, B, b0, lane, warp, [&](int r) { return (long)r; });
+    else gather(sxu, nx, (const T *)cand, B, b0, lane, warp, [&](int r) { return D.oX + (long)i * nx + r; });
+    gather(sdd, nu, DD, B, b0, lane, warp, [&](int r) { return (long)i * nu + r; });
+    if (R)
+        gather(sz, nZ, Z, B, b0, lane, warp, [&](int r) -> long {
+            if (r < nu) return (long)i * nu + r;
+            if (r < nu + nc * nx) return D.oX + (long)c0 * nx + (r - nu);
+            return D.oX + (r - nu - nc * nx);
+        });
+    cpAsyncWaitAll();
+    __syncthreads();
+    if (i == 0 && act)
+        for (int r = warp; r < nx; r += kTileWarps) {
+            const T x = sxu[r * kTileB + lane];
+            cand[ix(D.oX + r, B, b)] = x;
+            if (R) R[ix(D.oX + r, B, b)] = sz[(nu + nc * nx + r) * kTileB + lane] - x;
+        }
+    const int ldx = pad16(nx), ldu = pad16(nu);
+    T acc[kMaxTasks][kRT];
+    zeroAcc(acc);
+    gemv(acc, M.K + (size_t)i * ldu * nx, nu, nx, warp, [&](int k) { return sxu[k * kTileB + lane]; });
+    __syncthreads();  // every warp has read x before u is appended
+#pragma unroll
+    for (int q = 0; q < kMaxTasks; q++) {
+        const int r0 = (warp + q * kTileWarps) * kRT;
+#pragma unroll
+        for (int t = 0; t < kRT; t++) {
+            const int r = r0 + t;
+            if (r < nu) {
+                const T u = acc[q][t] + sdd[r * kTileB + lane];
+                sxu[(nx + r) * kTileB + lane] = u;
+                if (act) {
+                    cand[ix((long)i * nu + r, B, b)] = u;
+                    if (R) R[ix((long)i * nu + r, B, b)] = sz[r * kTileB + lane] - u;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    for (int jj = 0; jj < nc; jj++) {
+        const int j = c0 + jj;
+        zeroAcc(acc);
+        gemv(acc, M.AB + (size_t)j * ldx * nxu, nx, nxu, warp, [&](int k) { return sxu[k * kTileB + lane]; });
+        if (!act) continue;
+#pragma unroll
+        for (int q = 0; q < kMaxTasks; q++) {
+            const int r0 = (warp + q * kTileWarps) * kRT;
+#pragma unroll
+            for (int t = 0; t < kRT; t++) {
+                const int r = r0 + t;
+                if (r < nx) {
+                    const T x = acc[q][t] + (D.affine ? P.e[(size_t)j * nx + r] : T(0));
+                    cand[ix(D.oX + (long)j * nx + r, B, b)] = x;
+                    if (R) R[ix(D.oX + (long)j * nx + r, B, b)] = sz[(nu + jj * nx + r) * kTileB + lane] - x;
+                }
+            }
+        }
+    }
+}
+
+}  // namespace spock

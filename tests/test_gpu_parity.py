@@ -39,11 +39,15 @@ def rel(a, b):
     return np.abs(a - b).max() / max(1., np.abs(b).max())
 
 
+BATCHES = [1, 32]  # 1: per-row kernels (kernels.cuh); 32: batched kernels (kernels_batch.cuh)
+
+
 @pytest.mark.parametrize("case", CASES)
 @pytest.mark.parametrize("precision,tol", [(64, 1e-12), (32, 2e-5)])
-def test_operators(oracle_lib, case, precision, tol):
+@pytest.mark.parametrize("batch", BATCHES)
+def test_operators(oracle_lib, case, precision, tol, batch):
     path = os.path.join(GOLDEN, case)
-    t, d, c = make(path, precision)
+    t, d, c = make(path, precision, batch=batch)
     P = oracle_lib.Problem(path)
     prim = golden(case, "test_primBeforeOp_d.bt")
     dual = golden(case, "test_dualAfterOpBeforeAdj_d.bt")
@@ -60,10 +64,11 @@ def test_operators(oracle_lib, case, precision, tol):
 
 @pytest.mark.parametrize("case", CASES)
 @pytest.mark.parametrize("precision,tol", [(64, 1e-10), (32, 1e-4)])
-def test_cp_step(oracle_lib, case, precision, tol):
+@pytest.mark.parametrize("batch", BATCHES)
+def test_cp_step(oracle_lib, case, precision, tol, batch):
     """One Chambolle-Pock step T(z) (cache.cuh:795-801) from random iterates."""
     path = os.path.join(GOLDEN, case)
-    t, d, c = make(path, precision)
+    t, d, c = make(path, precision, batch=batch)
     P = oracle_lib.Problem(path)
     x0 = x0_of(case, P.nx)
     rng = np.random.default_rng(11)
@@ -98,8 +103,10 @@ def test_spock_solve_fp64(oracle_lib, case):
     z, s = P.run(x0, oracle_lib.options(tol=1e-3, max_iters=3000), "spock")
     assert s.status == 0
     assert abs(c.solveIter() - s.iters) <= 50
-    if c.solveIter() == s.iters:
-        assert rel(c.solution(), z) < 1e-6
+    # Both stop at the same relative tolerance; the GPU's Anderson step solves the Gram
+    # normal equations where the oracle uses Householder QR, so the trajectories agree only
+    # to the tolerance of the solve.
+    assert rel(c.solution(), z) < 5e-3
     u, xs = c.inputs(), c.states()
     u_ref, _ = P.states_inputs(z)[1], None
     assert np.abs(u[:P.nu] - u_ref[:P.nu]).max() < 5e-3 * max(1., np.abs(u_ref).max())
@@ -140,6 +147,25 @@ def test_batched_fp32_matches_single(oracle_lib):
         assert np.abs(u0[b] - u_ref).max() <= 2e-2 * max(1., np.abs(u_ref).max()), b
 
 
+@pytest.mark.parametrize("case", ["cfg1", "qpl"])
+def test_batched_kernels_solve(oracle_lib, case):
+    """64 instances through the batched kernels (FP32): all converge and their first inputs
+    match the oracle's FP64 solves.  (The reference test problem's terminal box |x| <= 0.1 is
+    infeasible for many random initial states, so it is not used here.)"""
+    path = os.path.join(GOLDEN, case)
+    P = oracle_lib.Problem(path)
+    rng = np.random.default_rng(8)
+    x0s = rng.uniform(-1, 1, (64, P.nx))
+    t, d, c = make(path, 32, batch=64, tol=1e-3, max_iters=3000)
+    st = c.runSpockBatch(x0s)
+    assert (st == 0).all()
+    u0 = c.firstInputs()
+    for b in range(0, 64, 9):
+        z, s = P.run(x0s[b], oracle_lib.options(tol=1e-3, max_iters=3000), "spock")
+        u_ref = P.states_inputs(z)[1][:P.nu]
+        assert np.abs(u0[b] - u_ref).max() <= 2e-2 * max(1., np.abs(u_ref).max()), b
+
+
 def test_batch_rows_reused_cyclically(oracle_lib):
     path = os.path.join(GOLDEN, "cfg1")
     t, d, c = make(path, 64, batch=4, tol=1e-3, max_iters=1000)
@@ -171,13 +197,14 @@ def test_unsupported_types_fail_loudly():
         sg.CacheBuilder(t, d).build()
 
 
-def test_full_size_operator_parity(oracle_lib, tmp_problems):
+@pytest.mark.parametrize("batch", BATCHES)
+def test_full_size_operator_parity(oracle_lib, tmp_problems, batch):
     """Config-2 sized problem (607 nodes, nx=50, nu=20): FP64 L, L*, T and M against the
     oracle, and the adjoint identity in FP32."""
     from spock_gb300 import configs
     path, x0 = configs.cached("config2", tmp_problems, seed=0, count=1)
     P = oracle_lib.Problem(path)
-    t, d, c = make(path, 64)
+    t, d, c = make(path, 64, batch=batch)
     rng = np.random.default_rng(2)
     p = rng.standard_normal(P.size_prim)
     q = rng.standard_normal(P.size_dual)
@@ -185,12 +212,13 @@ def test_full_size_operator_parity(oracle_lib, tmp_problems):
     assert rel(c.adj(q), P.adj(q)) < 1e-12
     z = rng.standard_normal(P.size)
     assert rel(c.cpStep(x0[0], z), P.cp_step(x0[0] * P.scaling[:P.nx], z)) < 1e-10
-    t32, d32, c32 = make(path, 32)
+    t32, d32, c32 = make(path, 32, batch=batch)
     lhs, rhs = q @ c32.op(p), c32.adj(q) @ p
     assert abs(lhs - rhs) <= 1e-4 * max(abs(lhs), 1.)
 
 
-def test_full_size_dynamics_feasible(oracle_lib, tmp_problems):
+@pytest.mark.parametrize("batch", BATCHES)
+def test_full_size_dynamics_feasible(oracle_lib, tmp_problems, batch):
     """After one FP32 CP step on a config-2 problem the candidate (x, u) satisfies the
     dynamics x_j = A_j x_anc(j) + B_j u_anc(j) and x_0 = x0 (the projection's defining
     property, dynamics.cuh:74-174)."""
@@ -198,7 +226,7 @@ def test_full_size_dynamics_feasible(oracle_lib, tmp_problems):
     from spock_gb300.factory import read_bt
     path, x0 = configs.cached("config2", tmp_problems, seed=0, count=1)
     P = oracle_lib.Problem(path)
-    t, d, c = make(path, 32)
+    t, d, c = make(path, 32, batch=batch)
     z = np.random.default_rng(4).standard_normal(P.size)
     cand = c.cpStep(x0[0], z)
     nx, nu, n, nnl = P.nx, P.nu, P.n, P.nnl
