@@ -759,18 +759,28 @@ private:
     }
 
     // Shared memory of the batched kernels (rows staged x 32 instances).
+    size_t lx() const { return (size_t)pad16(D_.nx); }
+    size_t lu() const { return (size_t)pad16(D_.nu); }
     size_t bLstar() const {
         const size_t in = (size_t)std::max(D_.ne * D_.dIV + D_.nxu + D_.yD + 1 + 2 * D_.ne, D_.dVI + D_.nx);
         const size_t base = (size_t)std::max(D_.nxu + D_.yD + 2 * D_.ne + 2, D_.nx);
-        return (in + base) * kTileB * sizeof(T);
+        const size_t mats = std::max((size_t)D_.ne * (lx() * D_.nx + lu() * D_.nu + lx() + lu()), lx() * D_.nx + lx());
+        return (mats + (in + base) * kTileB) * sizeof(T);
     }
     size_t bLop() const {
         const size_t in = (size_t)std::max(2 * D_.nxu + D_.yD + 2, D_.nxu + D_.nx + 2);
         const size_t base = (size_t)std::max(D_.yD + 1 + D_.nxu + D_.dIV, D_.dIV + D_.nx + D_.dVI);
-        return ((size_t)std::max(D_.dIV, D_.dVI) + 2 * in + base) * kTileB * sizeof(T);
+        const size_t mats = 2 * lx() * D_.nx + lu() * D_.nu;
+        return (mats + ((size_t)std::max(D_.dIV, D_.dVI) + 2 * in + base) * kTileB) * sizeof(T);
     }
-    size_t bBack() const { return (size_t)(D_.ne * D_.nx + 2 * D_.nu + D_.nx) * kTileB * sizeof(T); }
-    size_t bFwd() const { return (size_t)(D_.nxu + 2 * D_.nu + D_.ne * D_.nx + D_.nx) * kTileB * sizeof(T); }
+    size_t bBack() const {
+        const size_t mats = (size_t)D_.ne * (lu() * D_.nx + lx() * D_.nu + lx() * D_.nx) + lx() * D_.nu + lu() * D_.nu;
+        return (mats + (size_t)(D_.ne * D_.nx + 2 * D_.nu + D_.nx) * kTileB) * sizeof(T);
+    }
+    size_t bFwd() const {
+        const size_t mats = lu() * D_.nx + (size_t)D_.ne * lx() * D_.nxu;
+        return (mats + (size_t)(D_.nxu + 2 * D_.nu + D_.ne * D_.nx + D_.nx) * kTileB) * sizeof(T);
+    }
 
     void chooseKernels() {
         const int maxRows = kRT * kTileWarps * kMaxTasks;
@@ -790,6 +800,7 @@ private:
         M_.ABKTr = padUpload(p.ABKTr, nx, nx, p.numNodes);
         M_.Kt = padUpload(p.K, nx, nu, p.numNonleaf, true);  // K' from K (nu x nx)
         M_.K = padUpload(p.K, nu, nx, p.numNonleaf);
+        M_.chol = padUpload(p.lowChol, nu, nu, p.numNonleaf);
         M_.AB = padUpload(p.AB, nx, nx + nu, p.numNodes);
     }
 

@@ -6,10 +6,10 @@
 //     instances k*B + b0 .. b0+31 are one 128-byte coalesced segment) is copied into shared
 //     memory with cp.async, all issued before the first wait, so hundreds of loads are in
 //     flight per SM;
+//     The node's matrices, kept on the device with the leading dimension padded to a
+//     multiple of 16 rows, are copied to shared memory in the same asynchronous batch;
 //  2. compute: each warp accumulates blocks of 16 output rows in registers (16 FMAs per
-//     shared-memory input read); matrix columns are read as warp-uniform 16-byte loads from
-//     device copies whose leading dimension is padded to a multiple of 16 (L1/L2 resident,
-//     shared by all tiles of the node);
+//     shared-memory input read, matrix columns read as warp-uniform 16-byte loads);
 //  3. write: outputs (and, in a T evaluation, the residual Z - T(Z)) go out as coalesced rows.
 // Nothing in steps 2-3 reads global memory through a pointer that a store could alias.
 #pragma once
@@ -31,7 +31,7 @@ struct PadMats {
     const T *sqrtQ, *sqrtR, *q, *r;  // nonleaf cost, per node
     const T *lSqrtQ, *lq;            // leaf cost
     const T *BTr, *APB, *ABKTr;      // per node (child j)
-    const T *Kt, *K;                 // per nonleaf node: K' (nx x nu), K (nu x nx)
+    const T *Kt, *K, *chol;          // per nonleaf node: K' (nx x nu), K (nu x nx), lower Cholesky (nu x nu)
     const T *AB;                     // per node: [A B] (nx x nxu)
 };
 
@@ -45,17 +45,29 @@ __device__ __forceinline__ void cpAsyncElem(T *dst, const T *src) {
         asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smemAddr(dst)), "l"(src));
 }
 
+__device__ __forceinline__ void cpAsync16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smemAddr(dst)), "l"(src));
+}
+
+// Copy a padded matrix block (count elements, count * sizeof(T) a multiple of 16 bytes).
+template <typename T>
+__device__ __forceinline__ void stageMat(T *dst, const T *src, int count) {
+    const int chunks = count * (int)sizeof(T) / 16;
+    for (int c = threadIdx.x; c < chunks; c += blockDim.x)
+        cpAsync16(reinterpret_cast<char *>(dst) + 16 * (size_t)c, reinterpret_cast<const char *>(src) + 16 * (size_t)c);
+}
+
 __device__ __forceinline__ void cpAsyncWaitAll() {
     asm volatile("cp.async.commit_group;\n" ::);
     asm volatile("cp.async.wait_group 0;\n" ::);
 }
 
-// 16 consecutive matrix entries (16-byte aligned) as warp-uniform vector loads.
+// 16 consecutive matrix entries (16-byte aligned, shared memory) as warp-uniform vector loads.
 __device__ __forceinline__ void load16(const float *p, float v[kRT]) {
     const float4 *q = reinterpret_cast<const float4 *>(p);
 #pragma unroll
     for (int i = 0; i < 4; i++) {
-        const float4 a = __ldg(q + i);
+        const float4 a = q[i];
         v[4 * i] = a.x; v[4 * i + 1] = a.y; v[4 * i + 2] = a.z; v[4 * i + 3] = a.w;
     }
 }
@@ -64,7 +76,7 @@ __device__ __forceinline__ void load16(const double *p, double v[kRT]) {
     const double2 *q = reinterpret_cast<const double2 *>(p);
 #pragma unroll
     for (int i = 0; i < 8; i++) {
-        const double2 a = __ldg(q + i);
+        const double2 a = q[i];
         v[2 * i] = a.x; v[2 * i + 1] = a.y;
     }
 }
@@ -159,7 +171,26 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem
         return r == bRoot ? D.oT : D.oS;
     };
     const int inArr = A.in2 ? 2 : 1, baseArr = A.base2 ? 2 : (A.base1 ? 1 : 0);
-    T *sIn = sm, *sBase = sIn + nIn * inArr * kTileB;
+    const int ldx = pad16(nx), ldu = pad16(nu);
+    const int perChild = ldx * nx + ldu * nu + ldx + ldu;
+    const int matElems = nonleaf ? nc * perChild : ldx * nx + ldx;
+    T *sMat = sm, *sIn = sMat + matElems, *sBase = sIn + nIn * inArr * kTileB;
+    if (nonleaf) {
+        const bool qplNl = D.costNl == kCostQuadraticPlusLinear;
+        for (int jj = 0; jj < nc; jj++) {
+            const int j = c0 + jj;
+            T *m = sMat + jj * perChild;
+            stageMat(m, M.sqrtQ + (size_t)j * ldx * nx, ldx * nx);
+            stageMat(m + ldx * nx, M.sqrtR + (size_t)j * ldu * nu, ldu * nu);
+            if (qplNl) {
+                stageMat(m + ldx * nx + ldu * nu, M.q + (size_t)j * ldx, ldx);
+                stageMat(m + ldx * nx + ldu * nu + ldx, M.r + (size_t)j * ldu, ldu);
+            }
+        }
+    } else {
+        stageMat(sMat, M.lSqrtQ, ldx * nx);
+        if (D.costL == kCostQuadraticPlusLinear) stageMat(sMat + ldx * nx, M.lq, ldx);
+    }
     gather(sIn, nIn, A.in1, B, b0, lane, warp, rowIn);
     if (A.in2) gather(sIn + nIn * kTileB, nIn, A.in2, B, b0, lane, warp, rowIn);
     if (A.base1) gather(sBase, nBase, A.base1, B, b0, lane, warp, rowBase);
@@ -195,15 +226,15 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem
     zeroAcc(accU);
     if (nonleaf) {
         const bool qpl = D.costNl == kCostQuadraticPlusLinear;
-        const int ldx = pad16(nx), ldu = pad16(nu);
         for (int jj = 0; jj < nc; jj++) {
-            const int j = c0 + jj, r0 = jj * dIV;
-            gemv(accX, M.sqrtQ + (size_t)j * ldx * nx, nx, nx, warp, [&](int k) { return IN(r0 + k); });
-            gemv(accU, M.sqrtR + (size_t)j * ldu * nu, nu, nu, warp, [&](int k) { return IN(r0 + nx + k); });
+            const int r0 = jj * dIV;
+            const T *m = sMat + jj * perChild;
+            gemv(accX, m, nx, nx, warp, [&](int k) { return IN(r0 + k); });
+            gemv(accU, m + ldx * nx, nu, nu, warp, [&](int k) { return IN(r0 + nx + k); });
             if (qpl) {
                 const T d23 = T(-0.5) * (IN(r0 + nxu) + IN(r0 + nxu + 1));
-                gemv(accX, M.q + (size_t)j * ldx, nx, 1, warp, [&](int) { return d23; });
-                gemv(accU, M.r + (size_t)j * ldu, nu, 1, warp, [&](int) { return d23; });
+                gemv(accX, m + ldx * nx + ldu * nu, nx, 1, warp, [&](int) { return d23; });
+                gemv(accU, m + ldx * nx + ldu * nu + ldx, nu, 1, warp, [&](int) { return d23; });
             }
         }
 #pragma unroll
@@ -264,13 +295,11 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem
             }
         }
     } else {
-        const int ldx = pad16(nx);
-        gemv(accX, M.lSqrtQ, nx, nx, warp, [&](int k) { return IN(k); });
+        gemv(accX, sMat, nx, nx, warp, [&](int k) { return IN(k); });
         if (D.costL == kCostQuadraticPlusLinear) {
             const T d23 = T(-0.5) * (IN(nx) + IN(nx + 1));
-            gemv(accX, M.lq, nx, 1, warp, [&](int) { return d23; });
+            gemv(accX, sMat + ldx * nx, nx, 1, warp, [&](int) { return d23; });
         }
-        (void)ldx;
 #pragma unroll
         for (int q = 0; q < kMaxTasks; q++) {
             const int r0 = (warp + q * kTileWarps) * kRT;
@@ -336,7 +365,14 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T
     };
     const int inArr = A.in2 ? 2 : 1, baseArr = A.base2 ? 2 : (A.base1 ? 1 : 0);
     const int dSoc = dIV > dVI ? dIV : dVI;
-    T *sw = sm, *sIn = sw + dSoc * kTileB, *sBase = sIn + nIn * inArr * kTileB;
+    const int ldx = pad16(nx), ldu = pad16(nu);
+    const int matIV = ldx * nx + ldu * nu, matElems = matIV + (nonleaf ? 0 : ldx * nx);
+    T *sMat = sm, *sw = sMat + matElems, *sIn = sw + dSoc * kTileB, *sBase = sIn + nIn * inArr * kTileB;
+    if (j > 0) {
+        stageMat(sMat, M.sqrtQ + (size_t)j * ldx * nx, ldx * nx);
+        stageMat(sMat + ldx * nx, M.sqrtR + (size_t)j * ldu * nu, ldu * nu);
+    }
+    if (!nonleaf) stageMat(sMat + matIV, M.lSqrtQ, ldx * nx);
     gather(sIn, nIn, A.in1, B, b0, lane, warp, rowIn);
     if (A.in2) gather(sIn + nIn * kTileB, nIn, A.in2, B, b0, lane, warp, rowIn);
     if (A.base1) gather(sBase, nBase, A.base1, B, b0, lane, warp, rowBase);
@@ -416,9 +452,8 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T
         zeroAcc(accU);
         T h = 0;
         if (j > 0) {
-            const int ldx = pad16(nx), ldu = pad16(nu);
-            gemv(accX, M.sqrtQ + (size_t)j * ldx * nx, nx, nx, warp, [&](int k) { return INP(k); });
-            gemv(accU, M.sqrtR + (size_t)j * ldu * nu, nu, nu, warp, [&](int k) { return INP(nx + k); });
+            gemv(accX, sMat, nx, nx, warp, [&](int k) { return INP(k); });
+            gemv(accU, sMat + ldx * nx, nu, nu, warp, [&](int k) { return INP(nx + k); });
             h = T(0.5) * INP(nxu);
             if (D.costNl == kCostQuadraticPlusLinear) {
                 T lin = 0;
@@ -472,7 +507,7 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T
             }
         T accX[kMaxTasks][kRT];
         zeroAcc(accX);
-        gemv(accX, M.lSqrtQ, nx, nx, warp, [&](int k) { return INP(rx + k); });
+        gemv(accX, sMat + matIV, nx, nx, warp, [&](int k) { return INP(rx + k); });
         T h = T(0.5) * INP(rs);
         if (D.costL == kCostQuadraticPlusLinear) {
             T lin = 0;
@@ -527,7 +562,21 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_dyn_back_b(const DevProb
     const int nx = D.nx, nu = D.nu;
     const int c0 = P.chFrom[i], nc = P.numCh[i];
     const bool leafChildren = c0 >= D.nnl;
-    T *sq = sm, *su = sq + nc * nx * kTileB, *sx = su + nu * kTileB, *sd = sx + nx * kTileB;
+    const int ldx = pad16(nx), ldu = pad16(nu);
+    const int perChild = ldu * nx + ldx * nu + ldx * nx;  // B', APB, (A+BK)'
+    T *sMat = sm, *sKt = sMat + nc * perChild, *sL = sKt + ldx * nu;
+    T *sq = sL + ldu * nu, *su = sq + nc * nx * kTileB, *sx = su + nu * kTileB, *sd = sx + nx * kTileB;
+    for (int jj = 0; jj < nc; jj++) {
+        const int j = c0 + jj;
+        T *m = sMat + jj * perChild;
+        stageMat(m, M.BTr + (size_t)j * ldu * nx, ldu * nx);
+        if (stage > 0) {
+            stageMat(m + ldu * nx, M.APB + (size_t)j * ldx * nu, ldx * nu);
+            stageMat(m + ldu * nx + ldx * nu, M.ABKTr + (size_t)j * ldx * nx, ldx * nx);
+        }
+    }
+    if (stage > 0) stageMat(sKt, M.Kt + (size_t)i * ldx * nu, ldx * nu);
+    stageMat(sL, M.chol + (size_t)i * ldu * nu, ldu * nu);
     if (leafChildren)
         gather(sq, nc * nx, cand, B, b0, lane, warp, [&](int r) { return D.oX + (long)c0 * nx + r; });
     else
@@ -545,12 +594,11 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_dyn_back_b(const DevProb
         }
         __syncthreads();
     }
-    const int ldx = pad16(nx), ldu = pad16(nu);
     T acc[kMaxTasks][kRT];
     zeroAcc(acc);
     for (int jj = 0; jj < nc; jj++) {
         const T *qv = sq + jj * nx * kTileB + lane;
-        gemv(acc, M.BTr + (size_t)(c0 + jj) * ldu * nx, nu, nx, warp, [&](int k) { return qv[k * kTileB]; });
+        gemv(acc, sMat + jj * perChild, nu, nx, warp, [&](int k) { return qv[k * kTileB]; });
     }
 #pragma unroll
     for (int q = 0; q < kMaxTasks; q++) {
@@ -563,17 +611,17 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_dyn_back_b(const DevProb
     }
     __syncthreads();
     if (warp == 0) {  // (I + sum B'PB) d = rhs with the cached lower Cholesky factor
-        const T *L = P.chol + (size_t)i * nu * nu;
+        const T *L = sL;  // padded: L(r, k) at k * ldu + r
         T *v = sd + lane;
         for (int r = 0; r < nu; r++) {
             T s = v[r * kTileB];
-            for (int k = 0; k < r; k++) s -= __ldg(L + (size_t)k * nu + r) * v[k * kTileB];
-            v[r * kTileB] = s / __ldg(L + (size_t)r * nu + r);
+            for (int k = 0; k < r; k++) s -= L[k * ldu + r] * v[k * kTileB];
+            v[r * kTileB] = s / L[r * ldu + r];
         }
         for (int r = nu - 1; r >= 0; r--) {
             T s = v[r * kTileB];
-            for (int k = r + 1; k < nu; k++) s -= __ldg(L + (size_t)r * nu + k) * v[k * kTileB];
-            v[r * kTileB] = s / __ldg(L + (size_t)r * nu + r);
+            for (int k = r + 1; k < nu; k++) s -= L[r * ldu + k] * v[k * kTileB];
+            v[r * kTileB] = s / L[r * ldu + r];
         }
     }
     __syncthreads();
@@ -582,12 +630,12 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_dyn_back_b(const DevProb
     if (stage == 0) return;
     zeroAcc(acc);
     for (int jj = 0; jj < nc; jj++) {
-        const int j = c0 + jj;
+        const T *m = sMat + jj * perChild;
         const T *qv = sq + jj * nx * kTileB + lane;
-        gemv(acc, M.APB + (size_t)j * ldx * nu, nx, nu, warp, [&](int k) { return sd[k * kTileB + lane]; });
-        gemv(acc, M.ABKTr + (size_t)j * ldx * nx, nx, nx, warp, [&](int k) { return qv[k * kTileB]; });
+        gemv(acc, m + ldu * nx, nx, nu, warp, [&](int k) { return sd[k * kTileB + lane]; });
+        gemv(acc, m + ldu * nx + ldx * nu, nx, nx, warp, [&](int k) { return qv[k * kTileB]; });
     }
-    gemv(acc, M.Kt + (size_t)i * ldx * nu, nx, nu, warp,
+    gemv(acc, sKt, nx, nu, warp,
          [&](int k) { return sd[k * kTileB + lane] - su[k * kTileB + lane]; });
     if (!act) return;
 #pragma unroll
@@ -618,7 +666,11 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_dyn_fwd_b(const DevProbl
     const int i = stageFrom + blockIdx.y;
     const int nx = D.nx, nu = D.nu, nxu = D.nxu;
     const int c0 = P.chFrom[i], nc = P.numCh[i];
-    T *sxu = sm, *sdd = sxu + nxu * kTileB, *sz = sdd + nu * kTileB;  // sz: Z of [u_i][x_children][x_0]
+    const int ldx = pad16(nx), ldu = pad16(nu);
+    T *sK = sm, *sAB = sK + ldu * nx;
+    T *sxu = sAB + nc * ldx * nxu, *sdd = sxu + nxu * kTileB, *sz = sdd + nu * kTileB;  // sz: Z of [u_i][x_children][x_0]
+    stageMat(sK, M.K + (size_t)i * ldu * nx, ldu * nx);
+    for (int jj = 0; jj < nc; jj++) stageMat(sAB + jj * ldx * nxu, M.AB + (size_t)(c0 + jj) * ldx * nxu, ldx * nxu);
     const int nZ = nu + nc * nx + (i == 0 ? nx : 0);
     if (i == 0) gather(sxu, nx, x0s, B, b0, lane, warp, [&](int r) { return (long)r; });
     else gather(sxu, nx, (const T *)cand, B, b0, lane, warp, [&](int r) { return D.oX + (long)i * nx + r; });
@@ -637,10 +689,9 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_dyn_fwd_b(const DevProbl
             cand[ix(D.oX + r, B, b)] = x;
             if (R) R[ix(D.oX + r, B, b)] = sz[(nu + nc * nx + r) * kTileB + lane] - x;
         }
-    const int ldx = pad16(nx), ldu = pad16(nu);
     T acc[kMaxTasks][kRT];
     zeroAcc(acc);
-    gemv(acc, M.K + (size_t)i * ldu * nx, nu, nx, warp, [&](int k) { return sxu[k * kTileB + lane]; });
+    gemv(acc, sK, nu, nx, warp, [&](int k) { return sxu[k * kTileB + lane]; });
     __syncthreads();  // every warp has read x before u is appended
 #pragma unroll
     for (int q = 0; q < kMaxTasks; q++) {
@@ -662,7 +713,7 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_dyn_fwd_b(const DevProbl
     for (int jj = 0; jj < nc; jj++) {
         const int j = c0 + jj;
         zeroAcc(acc);
-        gemv(acc, M.AB + (size_t)j * ldx * nxu, nx, nxu, warp, [&](int k) { return sxu[k * kTileB + lane]; });
+        gemv(acc, sAB + jj * ldx * nxu, nx, nxu, warp, [&](int k) { return sxu[k * kTileB + lane]; });
         if (!act) continue;
 #pragma unroll
         for (int q = 0; q < kMaxTasks; q++) {
