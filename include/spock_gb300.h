@@ -110,6 +110,22 @@ int spock_round_time(spock_solver s, int rounds, double *ms);
  * last solve. */
 int spock_run_stats(spock_solver s, long *rounds, long *launches);
 
+/* Dynamics projection that allocates no device memory.  No counterpart in the reference: it
+ * is for callers that cannot allocate while they solve, such as a control loop re-solving
+ * under a hard deadline (a cudaMalloc's latency or failure is not acceptable there) or a host
+ * whose framework owns the device memory pool.  It projects one instance (u, x) onto the
+ * dynamics exactly like the projection inside spock_cp_step, in place, with the sweep's
+ * workspaces in a static 8 MiB device buffer built into the library.
+ *   s: a solver created with batch 1;  x0: the initial state in the solver's (preconditioned)
+ *   coordinates, nx device values;  prim_ux: device array [u (nu x numNonleaf) | x (nx x
+ *   numNodes)] in the solver precision, the head of a primal vector, overwritten with the
+ *   projection;  stream: a cudaStream_t (NULL for the default stream); returns when done.
+ * Problems whose workspaces (nx*numNodes + nu*numNonleaf values) exceed 8 MiB are rejected
+ * with SPOCK_E_INVALID.  The first call on a device looks up the buffer's device address, so
+ * make that first call before any stream capture.  All calls share the one buffer: calls that
+ * overlap on the GPU (other threads, other streams) race with each other. */
+int spock_project_dynamics_noalloc(spock_solver s, const void *x0, void *prim_ux, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

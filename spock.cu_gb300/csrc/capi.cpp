@@ -7,6 +7,7 @@
 #include <stdexcept>
 #include <string>
 
+#include "capi_internal.hpp"
 #include "engine.cuh"
 #include "problem.hpp"
 
@@ -289,3 +290,8 @@ int spock_run_stats(spock_solver sv, long *rounds, long *launches) {
 }
 
 }  // extern "C"
+
+namespace spock {
+EngineBase *engineOf(spock_solver s) { return solver(s)->eng.get(); }
+int guardedCall(const std::function<void()> &f) { return guard(f); }
+}  // namespace spock

@@ -396,6 +396,7 @@ public:
     Engine(const HostProblem &hp, const Options &opt, long batch, int device) {
         hp_ = hp;
         B_ = batch;
+        device_ = device;
         opt_ = opt;
         if (batch < 1) throw std::invalid_argument("[Cache] batch must be >= 1");
         if (opt.anderson < 1 || opt.anderson > kMaxAnderson)
@@ -651,6 +652,29 @@ public:
         }
         (void)nl;
         return 0;
+    }
+
+    void projectDynamicsOn(const void *x0, void *primUX, void *scratch, size_t scratchBytes,
+                           cudaStream_t stream) override {
+        if (B_ != 1) throw std::invalid_argument("[projectDynamics] needs a solver built with batch 1");
+        const size_t need = ((size_t)D_.nx * D_.n + (size_t)D_.nu * D_.nnl) * sizeof(T);
+        if (need > scratchBytes)
+            throw std::invalid_argument("[projectDynamics] problem needs " + std::to_string(need) +
+                                        " bytes of workspace, more than the " + std::to_string(scratchBytes) +
+                                        "-byte static buffer");
+        T *Q = static_cast<T *>(scratch), *DD = Q + (size_t)D_.nx * D_.n;
+        T *cand = static_cast<T *>(primUX);
+        const int N = D_.ns - 1;
+        for (int st = N - 1; st >= 0; st--) {
+            k_dyn_back<T><<<nodeGrid(stageCount_[st]), kNodeThreads, smBack(), stream>>>(P_, D_, cand, Q, DD, stageFrom_[st], st);
+            CK(cudaGetLastError());
+        }
+        for (int st = 0; st < N; st++) {
+            k_dyn_fwd<T><<<nodeGrid(stageCount_[st]), kNodeThreads, smFwd(), stream>>>(P_, D_, cand, DD, (const T *)x0,
+                                                                                       stageFrom_[st], nullptr, nullptr);
+            CK(cudaGetLastError());
+        }
+        CK(cudaStreamSynchronize(stream));
     }
 
     int launchesPerRound() const override { return 2 * (D_.ns - 1) + 2 + 2 + 3; }

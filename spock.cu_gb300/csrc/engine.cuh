@@ -97,6 +97,12 @@ public:
     virtual long bytesPerRoundAlgorithmic(const char *which) const = 0;
     virtual int launchesPerRound() const = 0;
     long lastRounds() const { return lastRounds_; }
+    int device() const { return device_; }
+    // Dynamics projection of a single-instance solver on caller-owned device memory: primUX is
+    // the head [u | x] of a primal vector (solver precision), x0 the scaled initial state, and
+    // the sweep's two workspaces live in `scratch` (scratchBytes long); runs on `stream`.
+    virtual void projectDynamicsOn(const void *x0, void *primUX, void *scratch, size_t scratchBytes,
+                                   cudaStream_t stream) = 0;
     long lastLaunches() const { return lastLaunches_; }
     const HostProblem &problem() const { return hp_; }
     long batch() const { return B_; }
@@ -105,6 +111,7 @@ protected:
     HostProblem hp_;
     long B_ = 1;
     long lastRounds_ = 0, lastLaunches_ = 0;
+    int device_ = 0;
 };
 
 EngineBase *makeEngine(const HostProblem &hp, const Options &opt, long batch, int precisionBits, int device);

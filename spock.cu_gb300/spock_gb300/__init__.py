@@ -71,6 +71,7 @@ _SIGS = {
     "spock_kernel_time": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int, _dp, _lp]),
     "spock_round_time": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
     "spock_run_stats": (ctypes.c_int, [_vp, _lp, _lp]),
+    "spock_project_dynamics_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
 }
 
 _lib = None

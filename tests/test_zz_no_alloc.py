@@ -1,0 +1,60 @@
+"""The allocation-free dynamics projection (spock_project_dynamics_noalloc).
+
+Callers that cannot allocate device memory while they solve (a control loop re-solving under
+a hard deadline, or a host whose framework owns the device memory pool) use this entry point:
+it keeps the projection's workspaces in a static device buffer.  Its result must equal the
+dynamics projection inside the existing spock_cp_step: with a zero dual part, T(z) leaves
+(u, x) equal to the projection of z's (u, x).  Checked twice in a row on each problem,
+FP64 to 1e-12 and FP32 to 2e-5 relative (the operator tolerances of test_gpu_parity.py).
+This file is collected last on purpose.
+"""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden
+
+import spock_gb300 as sg
+
+pytestmark = pytest.mark.gpu
+
+
+def _solver(case, precision):
+    t = sg.ScenarioTree(os.path.join(GOLDEN, case))
+    d = sg.ProblemData(t)
+    return t, d, sg.CacheBuilder(t, d).precision(precision).batch(1).build()
+
+
+@pytest.mark.parametrize("case,precision,tol", [("cfg1", 64, 1e-12), ("qpl", 64, 1e-12), ("qpl", 32, 2e-5)])
+def test_no_alloc_projection_matches_cp_step(case, precision, tol):
+    torch = pytest.importorskip("torch")
+    sg.build()
+    t, d, c = _solver(case, precision)
+    nx, nu, n, nnl = t.numStates(), t.numInputs(), t.numNodes(), t.numNonleafNodes()
+    head = nu * nnl + nx * n
+    dt = torch.float64 if precision == 64 else torch.float32
+    x0 = golden(case, "initialState_d.bt")
+    x0s = torch.tensor(x0 * d.scaling()[:nx], dtype=dt, device="cuda")
+    rng = np.random.default_rng(17)
+    for call in range(2):  # two calls in a row share the static workspace
+        z = np.zeros(c.sizeIterate())
+        z[:head] = 3 * rng.standard_normal(head)
+        ref = c.cpStep(x0, z)[:head]  # existing entry point
+        buf = torch.tensor(z[:head], dtype=dt, device="cuda")
+        torch.cuda.synchronize()
+        rc = sg.lib().spock_project_dynamics_noalloc(c._h, ctypes.c_void_p(x0s.data_ptr()),
+                                                      ctypes.c_void_p(buf.data_ptr()), None)
+        assert rc == 0, sg.lib().spock_last_error().decode()
+        out = buf.cpu().double().numpy()
+        assert np.abs(out - ref).max() <= tol * max(1., np.abs(ref).max()), call
+
+
+def test_no_alloc_rejects_batched_solver():
+    pytest.importorskip("torch")
+    t = sg.ScenarioTree(os.path.join(GOLDEN, "cfg1"))
+    d = sg.ProblemData(t)
+    c = sg.CacheBuilder(t, d).batch(2).build()
+    rc = sg.lib().spock_project_dynamics_noalloc(c._h, ctypes.c_void_p(1), ctypes.c_void_p(1), None)
+    assert rc == 1 and b"batch 1" in sg.lib().spock_last_error()
