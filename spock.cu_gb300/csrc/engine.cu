@@ -640,10 +640,13 @@ public:
         const long n = D_.n, nnl = D_.nnl, nl = D_.nl, nx = D_.nx, nu = D_.nu;
         const long matL = s * (n * (nx * nx + nu * nu) + nx * nx);          // sqrtQ, sqrtR, leaf sqrtQ
         const long matK = s * nnl * (long)D_.nd * D_.nd;                     // NNtr
-        if (w == "lop") return matL + s * B * (2 * D_.sPrim + 2 * D_.sDual);  // reads 2 prim + dual, writes dual
-        if (w == "lstar") return matL + matK + s * B * (D_.sDual + 2 * D_.sPrim);
-        if (w == "mlop") return matL + s * B * (2 * D_.sPrim + 2 * D_.sDual + 2 * D_.sDual);
-        if (w == "mlstar") return matL + s * B * (2 * D_.sDual + 2 * D_.sPrim + 2 * D_.sPrim);
+        const long sXU = nx * n + nu * nnl;  // x and u: their residual rows are written by the dynamics sweep
+        // T form of L: reads p and pbar, reads d, writes the candidate d and its residual
+        if (w == "lop") return matL + s * B * (2 * D_.sPrim + 3 * D_.sDual);
+        // T form of L*: reads d, reads p, writes the candidate p and the residual of y, t, s
+        if (w == "lstar") return matL + matK + s * B * (D_.sDual + 2 * D_.sPrim + (D_.sPrim - sXU));
+        if (w == "mlop") return matL + s * B * (D_.sPrim + 2 * D_.sDual);    // reads r_p, r_d; writes (Mr)_d
+        if (w == "mlstar") return matL + s * B * (D_.sDual + 2 * D_.sPrim);  // reads r_d, r_p; writes (Mr)_p
         if (w == "update") return s * B * D_.sZ * (5 + 7 + (opt_.anderson - 1));
         if (w == "reduce") return s * B * D_.sZ * (3 + opt_.anderson);
         if (w == "dyn") {
@@ -789,13 +792,13 @@ private:
         const size_t in = (size_t)std::max(D_.ne * D_.dIV + D_.nxu + D_.yD + 1 + 2 * D_.ne, D_.dVI + D_.nx);
         const size_t base = (size_t)std::max(D_.nxu + D_.yD + 2 * D_.ne + 2, D_.nx);
         const size_t mats = std::max((size_t)D_.ne * (lx() * D_.nx + lu() * D_.nu + lx() + lu()), lx() * D_.nx + lx());
-        return (mats + (in + base) * kTileB) * sizeof(T);
+        return (mats + (in + base + (size_t)D_.nd) * kTileB) * sizeof(T);
     }
     size_t bLop() const {
         const size_t in = (size_t)std::max(2 * D_.nxu + D_.yD + 2, D_.nxu + D_.nx + 2);
         const size_t base = (size_t)std::max(D_.yD + 1 + D_.nxu + D_.dIV, D_.dIV + D_.nx + D_.dVI);
         const size_t mats = 2 * lx() * D_.nx + lu() * D_.nu;
-        return (mats + ((size_t)std::max(D_.dIV, D_.dVI) + 2 * in + base) * kTileB) * sizeof(T);
+        return (mats + ((size_t)std::max(D_.dIV, D_.dVI) + kTileWarps + 2 * in + base) * kTileB) * sizeof(T);
     }
     size_t bBack() const {
         const size_t mats = (size_t)D_.ne * (lu() * D_.nx + lx() * D_.nu + lx() * D_.nx) + lx() * D_.nu + lu() * D_.nu;

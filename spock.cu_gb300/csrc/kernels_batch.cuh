@@ -19,11 +19,19 @@
 namespace spock {
 
 constexpr int kTileB = 32;     // instances per CTA (one per lane)
-constexpr int kTileWarps = 4;  // warps per CTA
+constexpr int kTileWarps = 8;  // warps per CTA
 constexpr int kRT = 16;        // output rows per register block
-constexpr int kMaxTasks = 2;   // register blocks per warp: rows <= 16 * 4 * 2 = 128
+constexpr int kMaxTasks = 2;   // register blocks per warp: rows <= 16 * 8 * 2 = 256
 
 __host__ __device__ inline int pad16(int r) { return (r + 15) & ~15; }
+
+// Register blocks of a matrix with `rows` rows, and the slot a warp takes in a matrix whose
+// blocks are dealt out starting at warp `first` (so two matrices accumulated side by side,
+// e.g. sqrt(Q) and sqrt(R), keep different warps busy).
+__host__ __device__ inline int tasksOf(int rows) { return pad16(rows) / kRT; }
+__device__ __forceinline__ int slotFrom(int warp, int first) {
+    return (warp - first % kTileWarps + kTileWarps) % kTileWarps;
+}
 
 // Pre-padded per-node matrices (column-major, leading dimension pad16(rows)).
 template <typename T>
@@ -89,14 +97,14 @@ __device__ __forceinline__ void zeroAcc(T acc[kMaxTasks][kRT]) {
         for (int t = 0; t < kRT; t++) acc[q][t] = T(0);
 }
 
-// acc[q][t] += sum_k M[(warp + 4q)*16 + t, k] * in(k), M padded column-major (ld = pad16(rows)).
+// acc[q][t] += sum_k M[(slot + 8q)*16 + t, k] * in(k), M padded column-major (ld = pad16(rows)).
 template <typename T, typename In>
-__device__ __forceinline__ void gemv(T acc[kMaxTasks][kRT], const T *M, int rows, int K, int warp, In in) {
+__device__ __forceinline__ void gemv(T acc[kMaxTasks][kRT], const T *M, int rows, int K, int slot, In in) {
     const int ld = pad16(rows);
     const int nTasks = ld / kRT;
 #pragma unroll
     for (int q = 0; q < kMaxTasks; q++) {
-        const int task = warp + q * kTileWarps;
+        const int task = slot + q * kTileWarps;
         if (task >= nTasks) continue;
         const T *col = M + task * kRT;
         int k = 0;
@@ -175,6 +183,7 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem
     const int perChild = ldx * nx + ldu * nu + ldx + ldu;
     const int matElems = nonleaf ? nc * perChild : ldx * nx + ldx;
     T *sMat = sm, *sIn = sMat + matElems, *sBase = sIn + nIn * inArr * kTileB;
+    T *sAv = sBase + nBase * baseArr * kTileB;  // the 4E+1 vector of the kernel projection
     if (nonleaf) {
         const bool qplNl = D.costNl == kCostQuadraticPlusLinear;
         for (int jj = 0; jj < nc; jj++) {
@@ -226,64 +235,66 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem
     zeroAcc(accU);
     if (nonleaf) {
         const bool qpl = D.costNl == kCostQuadraticPlusLinear;
+        const int sx = warp, su = slotFrom(warp, tasksOf(nx));  // x and u blocks on different warps
         for (int jj = 0; jj < nc; jj++) {
             const int r0 = jj * dIV;
             const T *m = sMat + jj * perChild;
-            gemv(accX, m, nx, nx, warp, [&](int k) { return IN(r0 + k); });
-            gemv(accU, m + ldx * nx, nu, nu, warp, [&](int k) { return IN(r0 + nx + k); });
+            gemv(accX, m, nx, nx, sx, [&](int k) { return IN(r0 + k); });
+            gemv(accU, m + ldx * nx, nu, nu, su, [&](int k) { return IN(r0 + nx + k); });
             if (qpl) {
                 const T d23 = T(-0.5) * (IN(r0 + nxu) + IN(r0 + nxu + 1));
-                gemv(accX, m + ldx * nx + ldu * nu, nx, 1, warp, [&](int) { return d23; });
-                gemv(accU, m + ldx * nx + ldu * nu + ldx, nu, 1, warp, [&](int) { return d23; });
+                gemv(accX, m + ldx * nx + ldu * nu, nx, 1, sx, [&](int) { return d23; });
+                gemv(accU, m + ldx * nx + ldu * nu + ldx, nu, 1, su, [&](int) { return d23; });
             }
         }
 #pragma unroll
         for (int q = 0; q < kMaxTasks; q++) {
-            const int r0 = (warp + q * kTileWarps) * kRT;
+            const int rx0 = (sx + q * kTileWarps) * kRT, ru0 = (su + q * kTileWarps) * kRT;
 #pragma unroll
             for (int t = 0; t < kRT; t++) {
-                const int r = r0 + t;
-                if (r < nx) EMIT(r, accX[q][t] + (rect ? IN(rIII + r) : T(0)));
-                if (r < nu) EMIT(nx + r, accU[q][t] + (rect ? IN(rIII + nx + r) : T(0)));
+                if (rx0 + t < nx) EMIT(rx0 + t, accX[q][t] + (rect ? IN(rIII + rx0 + t) : T(0)));
+                if (ru0 + t < nu) EMIT(nx + ru0 + t, accU[q][t] + (rect ? IN(rIII + nx + ru0 + t) : T(0)));
             }
         }
-        // y_i, the children's t and s, and the AVaR kernel projection (cache.cuh:650-676),
-        // one lane per instance on warp 0 (the 4E+1 vector is small)
+        // y_i, the children's t and s, and the AVaR kernel projection (cache.cuh:650-676): entry
+        // k of the 4E+1 vector is formed by warp k % 8; in a T evaluation it goes to shared
+        // memory and each warp then applies rows of N N' to it
+        const T II = IN(rII);
+        auto avarOut = [&](int k) -> int {  // base row of entry k, -1 for padding
+            if (k < yD) return bY + k;
+            if (k < yD + D.ne) return k - yD < nc ? bT + (k - yD) : -1;
+            return k - yD - D.ne < nc ? bS + (k - yD - D.ne) : -1;
+        };
+        auto avarLin = [&](int k) -> T {  // the L* part of entry k
+            if (k < yD) return IN(rI + k) - P.b[(size_t)i * yD + k] * II;
+            if (k < yD + D.ne) {
+                const int jj = k - yD;
+                return T(0.5) * (IN(jj * dIV + nxu) + IN(jj * dIV + nxu + 1));
+            }
+            const int jj = k - yD - D.ne;
+            return (c0 + jj < D.nnl) ? IN(rS + 2 * jj) : T(0.5) * (IN(rS + 2 * jj) + IN(rS + 2 * jj + 1));
+        };
+        if (MODE == 0) {
+            for (int k = warp; k < D.nd; k += kTileWarps) {
+                const int ob = avarOut(k);
+                sAv[k * kTileB + lane] = ob >= 0 ? BASE(ob) + A.cL * avarLin(k) : T(0);
+            }
+            __syncthreads();
+            const T *N = P.NNtr + (size_t)i * D.nd * D.nd;
+            for (int k = warp; k < D.nd; k += kTileWarps) {
+                const int ob = avarOut(k);
+                if (ob < 0) continue;
+                T acc = 0;
+                for (int c = 0; c < D.nd; c++) acc += __ldg(N + (size_t)c * D.nd + k) * sAv[c * kTileB + lane];
+                FIN(ob, acc);
+            }
+        } else {
+            for (int k = warp; k < D.nd; k += kTileWarps) {
+                const int ob = avarOut(k);
+                if (ob >= 0) EMIT(ob, avarLin(k));
+            }
+        }
         if (warp == 0) {
-            const T II = IN(rII);
-            T v[64];
-            int ob[64];
-            for (int k = 0; k < D.nd; k++) {
-                T lv = 0;
-                ob[k] = -1;
-                if (k < yD) {
-                    ob[k] = bY + k;
-                    lv = IN(rI + k) - P.b[(size_t)i * yD + k] * II;
-                } else if (k < yD + D.ne) {
-                    const int jj = k - yD;
-                    if (jj < nc) {
-                        ob[k] = bT + jj;
-                        lv = T(0.5) * (IN(jj * dIV + nxu) + IN(jj * dIV + nxu + 1));
-                    }
-                } else {
-                    const int jj = k - yD - D.ne;
-                    if (jj < nc) {
-                        ob[k] = bS + jj;
-                        lv = (c0 + jj < D.nnl) ? IN(rS + 2 * jj) : T(0.5) * (IN(rS + 2 * jj) + IN(rS + 2 * jj + 1));
-                    }
-                }
-                if (MODE == 0) v[k] = ob[k] >= 0 ? BASE(ob[k]) + A.cL * lv : T(0);
-                else if (ob[k] >= 0) EMIT(ob[k], lv);
-            }
-            if (MODE == 0) {
-                const T *N = P.NNtr + (size_t)i * D.nd * D.nd;
-                for (int k = 0; k < D.nd; k++) {
-                    if (ob[k] < 0) continue;
-                    T acc = 0;
-                    for (int c = 0; c < D.nd; c++) acc += __ldg(N + (size_t)c * D.nd + k) * v[c];
-                    FIN(ob[k], acc);
-                }
-            }
             if (i == 0) {  // t_0 carries no cost term; s_0 gets the prox of the objective
                 if (MODE == 0) {
                     FIN(bRoot, BASE(bRoot));
@@ -367,7 +378,8 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T
     const int dSoc = dIV > dVI ? dIV : dVI;
     const int ldx = pad16(nx), ldu = pad16(nu);
     const int matIV = ldx * nx + ldu * nu, matElems = matIV + (nonleaf ? 0 : ldx * nx);
-    T *sMat = sm, *sw = sMat + matElems, *sIn = sw + dSoc * kTileB, *sBase = sIn + nIn * inArr * kTileB;
+    T *sMat = sm, *sw = sMat + matElems, *sPart = sw + dSoc * kTileB;
+    T *sIn = sPart + kTileWarps * kTileB, *sBase = sIn + nIn * inArr * kTileB;
     if (j > 0) {
         stageMat(sMat, M.sqrtQ + (size_t)j * ldx * nx, ldx * nx);
         stageMat(sMat + ldx * nx, M.sqrtR + (size_t)j * ldu * nu, ldu * nu);
@@ -403,15 +415,20 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T
         A.out[o] = val;
         if (A.outR) A.outR[o] = BASE(rb) - val;
     };
-    // (v - proj(v)) * gamma for an SOC block staged in sw (dim rows), warp 0 only
+    // (v - proj(v)) * gamma for an SOC block staged in sw (dim rows), called by every warp after
+    // the barrier that publishes sw: the squared norm is summed over warps in shared memory
     auto socBlock = [&](int dim, int rb0) {
-        if (warp != 0) return;
         T ss = 0;
-        for (int c = 0; c < dim - 1; c++) ss += sw[c * kTileB + lane] * sw[c * kTileB + lane];
+        for (int c = warp; c < dim - 1; c += kTileWarps) ss += sw[c * kTileB + lane] * sw[c * kTileB + lane];
+        sPart[warp * kTileB + lane] = ss;
+        __syncthreads();
+        ss = 0;
+#pragma unroll
+        for (int w = 0; w < kTileWarps; w++) ss += sPart[w * kTileB + lane];
         const T nrm = sqrt(ss), tt = sw[(dim - 1) * kTileB + lane];
         const int i1 = nrm <= tt, i2 = (nrm <= -tt) && !i1, i3 = !i1 && !i2;
         const T sc = (nrm + tt) / (T(2) * nrm + T(1 - i3));
-        for (int c = 0; c < dim; c++) {
+        for (int c = warp; c < dim; c += kTileWarps) {
             const T v = sw[c * kTileB + lane];
             const T pr = i1 ? v : (i2 ? T(0) : (c < dim - 1 ? sc * v : sc * nrm));
             FIN(rb0 + c, (v - pr) * g);
@@ -451,9 +468,10 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T
         zeroAcc(accX);
         zeroAcc(accU);
         T h = 0;
+        const int sx = warp, su = slotFrom(warp, tasksOf(nx));  // x and u blocks on different warps
         if (j > 0) {
-            gemv(accX, sMat, nx, nx, warp, [&](int k) { return INP(k); });
-            gemv(accU, sMat + ldx * nx, nu, nu, warp, [&](int k) { return INP(nx + k); });
+            gemv(accX, sMat, nx, nx, sx, [&](int k) { return INP(k); });
+            gemv(accU, sMat + ldx * nx, nu, nu, su, [&](int k) { return INP(nx + k); });
             h = T(0.5) * INP(nxu);
             if (D.costNl == kCostQuadraticPlusLinear) {
                 T lin = 0;
@@ -465,14 +483,14 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T
         if (MODE == 0) {
 #pragma unroll
             for (int q = 0; q < kMaxTasks; q++) {
-                const int r0 = (warp + q * kTileWarps) * kRT;
+                const int rx0 = (sx + q * kTileWarps) * kRT, ru0 = (su + q * kTileWarps) * kRT;
 #pragma unroll
                 for (int t = 0; t < kRT; t++) {
-                    const int r = r0 + t;
+                    const int r = rx0 + t, ru = ru0 + t;
                     if (r < nx) sw[r * kTileB + lane] = (BASE(bIV + r) + A.cL * accX[q][t]) * gi + P.trans[(size_t)j * dIV + r];
-                    if (r < nu)
-                        sw[(nx + r) * kTileB + lane] =
-                            (BASE(bIV + nx + r) + A.cL * accU[q][t]) * gi + P.trans[(size_t)j * dIV + nx + r];
+                    if (ru < nu)
+                        sw[(nx + ru) * kTileB + lane] =
+                            (BASE(bIV + nx + ru) + A.cL * accU[q][t]) * gi + P.trans[(size_t)j * dIV + nx + ru];
                 }
             }
             if (warp == 0)
@@ -482,12 +500,11 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T
         } else {
 #pragma unroll
             for (int q = 0; q < kMaxTasks; q++) {
-                const int r0 = (warp + q * kTileWarps) * kRT;
+                const int rx0 = (sx + q * kTileWarps) * kRT, ru0 = (su + q * kTileWarps) * kRT;
 #pragma unroll
                 for (int t = 0; t < kRT; t++) {
-                    const int r = r0 + t;
-                    if (r < nx) EMIT(bIV + r, accX[q][t]);
-                    if (r < nu) EMIT(bIV + nx + r, accU[q][t]);
+                    if (rx0 + t < nx) EMIT(bIV + rx0 + t, accX[q][t]);
+                    if (ru0 + t < nu) EMIT(bIV + nx + ru0 + t, accU[q][t]);
                 }
             }
             if (warp == 0)
@@ -713,11 +730,12 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_dyn_fwd_b(const DevProbl
     for (int jj = 0; jj < nc; jj++) {
         const int j = c0 + jj;
         zeroAcc(acc);
-        gemv(acc, sAB + jj * ldx * nxu, nx, nxu, warp, [&](int k) { return sxu[k * kTileB + lane]; });
+        const int slot = slotFrom(warp, jj * tasksOf(nx));  // children's blocks on different warps
+        gemv(acc, sAB + jj * ldx * nxu, nx, nxu, slot, [&](int k) { return sxu[k * kTileB + lane]; });
         if (!act) continue;
 #pragma unroll
         for (int q = 0; q < kMaxTasks; q++) {
-            const int r0 = (warp + q * kTileWarps) * kRT;
+            const int r0 = (slot + q * kTileWarps) * kRT;
 #pragma unroll
             for (int t = 0; t < kRT; t++) {
                 const int r = r0 + t;
