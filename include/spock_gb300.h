@@ -79,6 +79,14 @@ int spock_solve(spock_solver s, int algo, const double *x0, long count, const do
  * element-major (x0[c * batch + b]); results stay on the device until read. */
 int spock_solve_device(spock_solver s, int algo, const void *x0_device, int *statuses, long *iters);
 
+/* Re-solve every instance warm-started from the solver's current iterate -- the solution of
+ * the previous solve, still on the device -- with new initial states: the reference's
+ * previousSolution warm start (cache.cuh:611-632) for a control loop that re-solves as the state
+ * moves, without sending iterates through the host.  x0 as in spock_solve (host, unscaled) or
+ * spock_solve_device (device, solver precision).  After spock_reset the iterate is zero. */
+int spock_resolve(spock_solver s, int algo, const double *x0, long count, int *statuses, long *iters);
+int spock_resolve_device(spock_solver s, int algo, const void *x0_device, int *statuses, long *iters);
+
 /* Results.  Cache::solution() (cache.cuh:378): the raw iterate of one instance, sizePrimal +
  * sizeDual doubles.  Cache::states()/inputs() (cache.cuh:386-412): unscaled, nx*numNodes and
  * nu*numNonleafNodes doubles.  first_inputs: the unscaled u_0 of every instance (batch*nu). */
@@ -109,6 +117,10 @@ int spock_round_time(spock_solver s, int rounds, double *ms);
 /* Rounds (one T evaluation + one M application per instance each) and kernel launches of the
  * last solve. */
 int spock_run_stats(spock_solver s, long *rounds, long *launches);
+/* Tile shapes the built-in autotuner chose for L* and L (it times 1, 2, 4 and 8 instance tiles
+ * per CTA once, before the first solve): out5 = {L* tiles per CTA, L* double-buffered, L tiles
+ * per CTA, L double-buffered, batched kernels in use}.  No reference counterpart. */
+int spock_tuning(spock_solver s, int *out5);
 
 /* Dynamics projection that allocates no device memory.  No counterpart in the reference: it
  * is for callers that cannot allocate while they solve, such as a control loop re-solving

@@ -123,6 +123,17 @@ class Cache {
         return status_;
     }
 
+    // Re-solve warm-started from the current iterate (the previous solution, kept on the device)
+    // with new initial states: the control-loop form of runSpock(x0, &previousSolution).
+    std::vector<int> resolveBatch(const std::vector<T> &initStates) {
+        const long count = (long)(initStates.size() / tree_.numStates());
+        if (count < 1 || initStates.size() != tree_.numStates() * (size_t)count)
+            throw std::invalid_argument("[initialiseState] wrong number of states");
+        std::vector<double> x(initStates.begin(), initStates.end());
+        check(spock_resolve(h_.get(), SPOCK_ALGO_SPOCK, x.data(), count, status_.data(), iters_.data()));
+        return status_;
+    }
+
     int status(long instance = 0) const { return status_[(size_t)instance]; }
     size_t solveIter(long instance = 0) const { return (size_t)iters_[(size_t)instance]; }
     T solveTime() const {

@@ -1011,6 +1011,7 @@ typedef struct {
     long *iters;
     double *u0;
     double *zs;
+    int warm;
 } Job;
 
 static void *job_run(void *arg) {
@@ -1019,7 +1020,8 @@ static void *job_run(void *arg) {
     double *z = (double *)malloc(sizeof(double) * (size_t)p->sZ);
     for (long k = j->begin; k < j->end; k++) {
         OrStats st;
-        or_run_spock(p, j->o, j->x0s + k * p->nx, z, 0, &st);
+        if (j->warm) memcpy(z, j->zs + k * p->sZ, sizeof(double) * (size_t)p->sZ);
+        or_run_spock(p, j->o, j->x0s + k * p->nx, z, j->warm, &st);
         j->status[k] = st.status;
         j->iters[k] = st.iters;
         for (long q = 0; q < p->nu; q++) j->u0[k * p->nu + q] = z[q] / p->scaling[p->nx + q];
@@ -1031,6 +1033,12 @@ static void *job_run(void *arg) {
 
 double or_solve_many(const OrProblem *p, const OrOptions *o, long count, const double *x0s, int threads,
                      int *status, long *iters, double *u0, double *zs) {
+    return or_solve_many_warm(p, o, count, x0s, threads, status, iters, u0, zs, 0);
+}
+
+double or_solve_many_warm(const OrProblem *p, const OrOptions *o, long count, const double *x0s, int threads,
+                          int *status, long *iters, double *u0, double *zs, int warm) {
+    if (warm && !zs) return -1.;
     if (threads < 1) threads = 1;
     if (threads > count) threads = (int)count;
     pthread_t th[256];
@@ -1039,7 +1047,7 @@ double or_solve_many(const OrProblem *p, const OrOptions *o, long count, const d
     const double t0 = now_s();
     for (int t = 0; t < threads; t++) {
         jobs[t].p = p; jobs[t].o = o; jobs[t].x0s = x0s; jobs[t].status = status; jobs[t].iters = iters;
-        jobs[t].u0 = u0; jobs[t].zs = zs;
+        jobs[t].u0 = u0; jobs[t].zs = zs; jobs[t].warm = warm;
         jobs[t].begin = count * t / threads;
         jobs[t].end = count * (t + 1) / threads;
         pthread_create(&th[t], NULL, job_run, &jobs[t]);

@@ -74,6 +74,10 @@ void or_states_inputs(const OrProblem *p, const double *z, double *states, doubl
  * iteration counts and the first-stage input of each instance (count*nu).  Returns wall s. */
 double or_solve_many(const OrProblem *p, const OrOptions *o, long count, const double *x0s,
                      int threads, int *status, long *iters, double *u0, double *zs_or_null);
+/* Same; with warm != 0 each instance starts from its iterate in zs (count*sZ, required) -- the
+ * previousSolution warm start of cache.cuh:611-632 -- and zs receives the solutions. */
+double or_solve_many_warm(const OrProblem *p, const OrOptions *o, long count, const double *x0s,
+                          int threads, int *status, long *iters, double *u0, double *zs, int warm);
 
 /* Offline dynamics cache (problem.py:192-213) from per-node [A B] (nx x (nx+nu) x n):
  * writes P (nx*nx*n), K (nu*nx*nnl), lowChol (nu*nu*nnl), ABKTr (nx*nx*n), APB (nx*nu*n). */

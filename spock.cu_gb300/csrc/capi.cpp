@@ -161,6 +161,28 @@ int spock_solve_device(spock_solver sv, int algo, const void *x0, int *statuses,
     });
 }
 
+int spock_resolve(spock_solver sv, int algo, const double *x0, long count, int *statuses, long *iters) {
+    return guard([&] {
+        auto *s = solver(sv);
+        need(x0, "x0");
+        if (algo != SPOCK_ALGO_SPOCK && algo != SPOCK_ALGO_CP) throw std::invalid_argument("[Cache] unknown algorithm");
+        s->eng->setInitialStates(x0, count);
+        s->eng->run(algo == SPOCK_ALGO_SPOCK ? spock::kSpock : spock::kCp, true);
+        finishSolve(s, statuses, iters);
+    });
+}
+
+int spock_resolve_device(spock_solver sv, int algo, const void *x0, int *statuses, long *iters) {
+    return guard([&] {
+        auto *s = solver(sv);
+        need(x0, "x0");
+        if (algo != SPOCK_ALGO_SPOCK && algo != SPOCK_ALGO_CP) throw std::invalid_argument("[Cache] unknown algorithm");
+        s->eng->setInitialStatesDevice(x0, s->eng->batch());
+        s->eng->run(algo == SPOCK_ALGO_SPOCK ? spock::kSpock : spock::kCp, true);
+        finishSolve(s, statuses, iters);
+    });
+}
+
 int spock_get_iterate(spock_solver sv, long instance, double *out) {
     return guard([&] {
         auto *s = solver(sv);
@@ -286,6 +308,13 @@ int spock_run_stats(spock_solver sv, long *rounds, long *launches) {
         auto *s = solver(sv);
         if (rounds) *rounds = s->eng->lastRounds();
         if (launches) *launches = s->eng->lastLaunches();
+    });
+}
+
+int spock_tuning(spock_solver sv, int *out5) {
+    return guard([&] {
+        if (!out5) throw std::invalid_argument("[spock_tuning] null output");
+        solver(sv)->eng->tuning(out5);
     });
 }
 

@@ -585,7 +585,13 @@ public:
         downloadSlice(MR_, mz, 0, D_.sZ);
     }
 
+    void tuning(int *out5) override {
+        autotune();
+        out5[0] = tpcLstar_; out5[1] = lstarDbl_; out5[2] = tpcLop_; out5[3] = lopDbl_; out5[4] = batched_;
+    }
+
     double kernelMs(const char *which, int reps) override {
+        autotune();
         cudaEvent_t e0, e1;
         CK(cudaEventCreate(&e0));
         CK(cudaEventCreate(&e1));
@@ -688,6 +694,10 @@ private:
     DevProblem<T> P_{};
     PadMats<T> M_{};
     bool batched_ = false;  // kernels_batch.cuh for >= 32 instances, kernels.cuh otherwise
+    bool lstarDbl_ = false, lopDbl_ = false;  // L*, L double-buffer their instance tiles
+    int tpcLstar_ = 1, tpcLop_ = 1;           // instance tiles per L* / L CTA (autotune())
+    bool tuned_ = false;
+    static constexpr int kTilesPerCta = 8;
     DevState S_{};
     cudaStream_t stream_ = nullptr;
     cudaGraphExec_t graph_ = nullptr;
@@ -788,18 +798,25 @@ private:
     // Shared memory of the batched kernels (rows staged x 32 instances).
     size_t lx() const { return (size_t)pad16(D_.nx); }
     size_t lu() const { return (size_t)pad16(D_.nu); }
-    size_t bLstar() const {
+    // L* and L stage the node's matrices once and one (or, double-buffered, two) instance
+    // tiles of input and base rows.
+    size_t bLstar(bool dbl = false) const {
         const size_t in = (size_t)std::max(D_.ne * D_.dIV + D_.nxu + D_.yD + 1 + 2 * D_.ne, D_.dVI + D_.nx);
         const size_t base = (size_t)std::max(D_.nxu + D_.yD + 2 * D_.ne + 2, D_.nx);
         const size_t mats = std::max((size_t)D_.ne * (lx() * D_.nx + lu() * D_.nu + lx() + lu()), lx() * D_.nx + lx());
-        return (mats + (in + base + (size_t)D_.nd) * kTileB) * sizeof(T);
+        return (mats + ((dbl ? 2 : 1) * (in + base) + (size_t)D_.nd) * kTileB) * sizeof(T);
     }
-    size_t bLop() const {
+    size_t bLop(bool dbl = false) const {
         const size_t in = (size_t)std::max(2 * D_.nxu + D_.yD + 2, D_.nxu + D_.nx + 2);
         const size_t base = (size_t)std::max(D_.yD + 1 + D_.nxu + D_.dIV, D_.dIV + D_.nx + D_.dVI);
         const size_t mats = 2 * lx() * D_.nx + lu() * D_.nu;
-        return (mats + ((size_t)std::max(D_.dIV, D_.dVI) + kTileWarps + 2 * in + base) * kTileB) * sizeof(T);
+        return (mats + ((size_t)std::max(D_.dIV, D_.dVI) + kTileWarps + (dbl ? 2 : 1) * (2 * in + base)) * kTileB) *
+               sizeof(T);
     }
+    size_t smLstarB() const { return bLstar(lstarDbl_); }
+    size_t smLopB() const { return bLop(lopDbl_); }
+    bool canDblLstar() const { return bLstar(true) <= 220 * 1024; }
+    bool canDblLop() const { return bLop(true) <= 220 * 1024; }
     size_t bBack() const {
         const size_t mats = (size_t)D_.ne * (lu() * D_.nx + lx() * D_.nu + lx() * D_.nx) + lx() * D_.nu + lu() * D_.nu;
         return (mats + (size_t)(D_.ne * D_.nx + 2 * D_.nu + D_.nx) * kTileB) * sizeof(T);
@@ -879,12 +896,13 @@ private:
 
     void raiseSharedLimits() {
         if (batched_) {
-            optIn(k_lstar_b<T, 0>, bLstar());
-            optIn(k_lstar_b<T, 1>, bLstar());
-            optIn(k_lstar_b<T, 2>, bLstar());
-            optIn(k_lop_b<T, 0>, bLop());
-            optIn(k_lop_b<T, 1>, bLop());
-            optIn(k_lop_b<T, 2>, bLop());
+            // the limit covers the largest shape the tuner may pick
+            optIn(k_lstar_b<T, 0>, bLstar(canDblLstar()));
+            optIn(k_lstar_b<T, 1>, bLstar(canDblLstar()));
+            optIn(k_lstar_b<T, 2>, bLstar(canDblLstar()));
+            optIn(k_lop_b<T, 0>, bLop(canDblLop()));
+            optIn(k_lop_b<T, 1>, bLop(canDblLop()));
+            optIn(k_lop_b<T, 2>, bLop(canDblLop()));
             optIn(k_dyn_back_b<T>, bBack());
             optIn(k_dyn_fwd_b<T>, bFwd());
             return;
@@ -963,10 +981,57 @@ private:
 
     dim3 tileGrid(int nodes) const { return dim3((unsigned)((B_ + kTileB - 1) / kTileB), (unsigned)nodes); }
 
+    // L and L*: every node x groups of `tpc` instance tiles.
+    dim3 opGrid(int tpc) const {
+        const long tiles = (B_ + kTileB - 1) / kTileB;
+        return dim3((unsigned)((tiles + tpc - 1) / tpc), (unsigned)D_.n);
+    }
+
+    // Autotuner of the L / L* tile shape: instance tiles per CTA in {1, 2, 4, 8}, double-buffered
+    // when more than one and the shared memory allows.  Each candidate is timed over 3 launches
+    // of the T-form kernel (CUDA events on the solver stream); the fastest is kept.  Runs once,
+    // before the round is captured; it writes only CAND and R, which every round rewrites first.
+    void autotune() {
+        if (!batched_ || tuned_) return;
+        tuned_ = true;
+        const int tiles = (int)((B_ + kTileB - 1) / kTileB);
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        auto timeIt = [&](auto launch) {
+            launch();
+            CK(cudaEventRecord(e0, stream_));
+            for (int r = 0; r < 3; r++) launch();
+            CK(cudaEventRecord(e1, stream_));
+            CK(cudaEventSynchronize(e1));
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            return ms;
+        };
+        float bestS = 1e30f, bestL = 1e30f;
+        int tS = 1, tL = 1;
+        for (int tpc = 1; tpc <= kTilesPerCta && tpc <= tiles; tpc *= 2) {
+            tpcLstar_ = tpcLop_ = tpc;
+            lstarDbl_ = tpc > 1 && canDblLstar();
+            lopDbl_ = tpc > 1 && canDblLop();
+            const float ms = timeIt([&] { launchLstar<0>(tevalLstarArgs()); });
+            if (ms < bestS) { bestS = ms; tS = tpc; }
+            const float ml = timeIt([&] { launchLop<0>(tevalLopArgs()); });
+            if (ml < bestL) { bestL = ml; tL = tpc; }
+        }
+        tpcLstar_ = tS;
+        lstarDbl_ = tS > 1 && canDblLstar();
+        tpcLop_ = tL;
+        lopDbl_ = tL > 1 && canDblLop();
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+
     template <int MODE>
     void launchLstar(const OpArgs<T> &A) {
         if (batched_) {
-            k_lstar_b<T, MODE><<<tileGrid(D_.n), kTileB * kTileWarps, bLstar(), stream_>>>(P_, D_, A, M_);
+            k_lstar_b<T, MODE><<<opGrid(tpcLstar_), kTileB * kTileWarps, smLstarB(), stream_>>>(P_, D_, A, M_, tpcLstar_,
+                                                                                                (int)lstarDbl_);
             CK(cudaGetLastError());
             return;
         }
@@ -977,7 +1042,8 @@ private:
     template <int MODE>
     void launchLop(const OpArgs<T> &A) {
         if (batched_) {
-            k_lop_b<T, MODE><<<tileGrid(D_.n), kTileB * kTileWarps, bLop(), stream_>>>(P_, D_, A, M_);
+            k_lop_b<T, MODE><<<opGrid(tpcLop_), kTileB * kTileWarps, smLopB(), stream_>>>(P_, D_, A, M_, tpcLop_,
+                                                                                          (int)lopDbl_);
             CK(cudaGetLastError());
             return;
         }
@@ -1075,6 +1141,7 @@ private:
 
     void ensureGraph() {
         if (graph_) return;
+        autotune();
         cudaGraph_t g;
         CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
         roundSpock();

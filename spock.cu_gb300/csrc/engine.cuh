@@ -96,6 +96,9 @@ public:
     virtual void timedRounds(int rounds, float *ms) = 0;
     virtual long bytesPerRoundAlgorithmic(const char *which) const = 0;
     virtual int launchesPerRound() const = 0;
+    // Tile shapes in use: L* instance tiles per CTA, L* double-buffered, the same for L,
+    // batched kernels (1) or the small-batch ones (0).  Runs the autotuner if it has not run.
+    virtual void tuning(int *out5) = 0;
     long lastRounds() const { return lastRounds_; }
     int device() const { return device_; }
     // Dynamics projection of a single-instance solver on caller-owned device memory: primUX is

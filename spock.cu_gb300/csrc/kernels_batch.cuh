@@ -69,6 +69,12 @@ __device__ __forceinline__ void cpAsyncWaitAll() {
     asm volatile("cp.async.commit_group;\n" ::);
     asm volatile("cp.async.wait_group 0;\n" ::);
 }
+__device__ __forceinline__ void cpAsyncCommit() { asm volatile("cp.async.commit_group;\n" ::); }
+// Wait for every group but the most recent one (double buffering) or for all of them.
+__device__ __forceinline__ void cpAsyncWaitPrev(bool dbl) {
+    if (dbl) asm volatile("cp.async.wait_group 1;\n" ::);
+    else asm volatile("cp.async.wait_group 0;\n" ::);
+}
 
 // 16 consecutive matrix entries (16-byte aligned, shared memory) as warp-uniform vector loads.
 __device__ __forceinline__ void load16(const float *p, float v[kRT]) {
@@ -97,6 +103,26 @@ __device__ __forceinline__ void zeroAcc(T acc[kMaxTasks][kRT]) {
         for (int t = 0; t < kRT; t++) acc[q][t] = T(0);
 }
 
+// acc[t] += m[t] * v for the 16 rows of a register block.  FP32 uses the packed two-lane FMA
+// (fma.rn.f32x2, one instruction for two rows): each lane is an IEEE fused multiply-add
+// rounded to nearest, bit-identical to the scalar FMA it replaces, with half the issue slots.
+__device__ __forceinline__ void axpy16(float acc[kRT], const float m[kRT], float v) {
+    unsigned long long vv;
+    asm("mov.b64 %0, {%1, %1};" : "=l"(vv) : "f"(v));
+#pragma unroll
+    for (int t = 0; t < kRT; t += 2) {
+        unsigned long long a, mm;
+        asm("mov.b64 %0, {%1, %2};" : "=l"(a) : "f"(acc[t]), "f"(acc[t + 1]));
+        asm("mov.b64 %0, {%1, %2};" : "=l"(mm) : "f"(m[t]), "f"(m[t + 1]));
+        asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(a) : "l"(mm), "l"(vv));
+        asm("mov.b64 {%0, %1}, %2;" : "=f"(acc[t]), "=f"(acc[t + 1]) : "l"(a));
+    }
+}
+__device__ __forceinline__ void axpy16(double acc[kRT], const double m[kRT], double v) {
+#pragma unroll
+    for (int t = 0; t < kRT; t++) acc[t] = fma(m[t], v, acc[t]);
+}
+
 // acc[q][t] += sum_k M[(slot + 8q)*16 + t, k] * in(k), M padded column-major (ld = pad16(rows)).
 template <typename T, typename In>
 __device__ __forceinline__ void gemv(T acc[kMaxTasks][kRT], const T *M, int rows, int K, int slot, In in) {
@@ -113,17 +139,13 @@ __device__ __forceinline__ void gemv(T acc[kMaxTasks][kRT], const T *M, int rows
             load16(col + (size_t)k * ld, m0);
             load16(col + (size_t)(k + 1) * ld, m1);
             const T v0 = in(k), v1 = in(k + 1);
-#pragma unroll
-            for (int t = 0; t < kRT; t++) acc[q][t] += m0[t] * v0;
-#pragma unroll
-            for (int t = 0; t < kRT; t++) acc[q][t] += m1[t] * v1;
+            axpy16(acc[q], m0, v0);
+            axpy16(acc[q], m1, v1);
         }
         if (k < K) {
             T m0[kRT];
             load16(col + (size_t)k * ld, m0);
-            const T v0 = in(k);
-#pragma unroll
-            for (int t = 0; t < kRT; t++) acc[q][t] += m0[t] * v0;
+            axpy16(acc[q], m0, in(k));
         }
     }
 }
@@ -143,12 +165,10 @@ __device__ __forceinline__ void gather(T *sm, int n, const T *src, int B, int b0
 // ------------------------------------------------------------------------------------------
 template <typename T, int MODE>
 __global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem<T> P, const Dims D, const OpArgs<T> A,
-                                                                const PadMats<T> M) {
+                                                                const PadMats<T> M, int tilesPerCta, int dbl) {
     extern __shared__ __align__(16) unsigned char smraw[];
     T *sm = reinterpret_cast<T *>(smraw);
     const int B = D.B, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int b0 = blockIdx.x * kTileB, b = b0 + lane;
-    const bool act = b < B;
     const int i = blockIdx.y;
     const int nx = D.nx, nu = D.nu, nxu = D.nxu, dIV = D.dIV, dVI = D.dVI, yD = D.yD;
     const bool nonleaf = i < D.nnl;
@@ -182,8 +202,9 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem
     const int ldx = pad16(nx), ldu = pad16(nu);
     const int perChild = ldx * nx + ldu * nu + ldx + ldu;
     const int matElems = nonleaf ? nc * perChild : ldx * nx + ldx;
-    T *sMat = sm, *sIn = sMat + matElems, *sBase = sIn + nIn * inArr * kTileB;
-    T *sAv = sBase + nBase * baseArr * kTileB;  // the 4E+1 vector of the kernel projection
+    const int bufElems = (nIn * inArr + nBase * baseArr) * kTileB;  // one tile's input and base rows
+    T *sMat = sm, *sBuf = sMat + matElems;
+    T *sAv = sBuf + (dbl ? 2 : 1) * bufElems;  // the 4E+1 vector of the kernel projection
     if (nonleaf) {
         const bool qplNl = D.costNl == kCostQuadraticPlusLinear;
         for (int jj = 0; jj < nc; jj++) {
@@ -200,126 +221,146 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem
         stageMat(sMat, M.lSqrtQ, ldx * nx);
         if (D.costL == kCostQuadraticPlusLinear) stageMat(sMat + ldx * nx, M.lq, ldx);
     }
-    gather(sIn, nIn, A.in1, B, b0, lane, warp, rowIn);
-    if (A.in2) gather(sIn + nIn * kTileB, nIn, A.in2, B, b0, lane, warp, rowIn);
-    if (A.base1) gather(sBase, nBase, A.base1, B, b0, lane, warp, rowBase);
-    if (A.base2) gather(sBase + nBase * kTileB, nBase, A.base2, B, b0, lane, warp, rowBase);
-    cpAsyncWaitAll();
-    __syncthreads();
-    auto IN = [&](int r) -> T {
-        T v = A.a1 * sIn[r * kTileB + lane];
-        if (inArr == 2) v += A.a2 * sIn[(nIn + r) * kTileB + lane];
-        return v;
+    // This CTA's instance tiles [t0, t1): with double buffering the rows of tile t + 1 are in
+    // flight while tile t is computed; the node's matrices are staged once for all of them.
+    const int nTiles = (B + kTileB - 1) / kTileB;
+    const int t0 = blockIdx.x * tilesPerCta, t1 = min(t0 + tilesPerCta, nTiles);
+    auto prefetch = [&](int t) {
+        T *buf = sBuf + (dbl ? ((t - t0) & 1) * bufElems : 0);
+        const int bb = t * kTileB;
+        gather(buf, nIn, A.in1, B, bb, lane, warp, rowIn);
+        if (A.in2) gather(buf + nIn * kTileB, nIn, A.in2, B, bb, lane, warp, rowIn);
+        T *bs = buf + nIn * inArr * kTileB;
+        if (A.base1) gather(bs, nBase, A.base1, B, bb, lane, warp, rowBase);
+        if (A.base2) gather(bs + nBase * kTileB, nBase, A.base2, B, bb, lane, warp, rowBase);
     };
-    auto BASE = [&](int r) -> T {
-        if (!baseArr) return T(0);
-        T v = A.b1 * sBase[r * kTileB + lane];
-        if (baseArr == 2) v += A.b2 * sBase[(nBase + r) * kTileB + lane];
-        return v;
-    };
-    auto EMIT = [&](int rb, T lv) {
-        if (!act) return;
-        const T bs = BASE(rb);
-        const size_t o = (size_t)rowBase(rb) * B + b;
-        if (A.outBase) A.outBase[o] = bs;
-        A.out[o] = bs + A.cL * lv;
-    };
-    auto FIN = [&](int rb, T val) {  // a final primal entry (mode 0) and its residual
-        if (!act) return;
-        const size_t o = (size_t)rowBase(rb) * B + b;
-        A.out[o] = val;
-        if (A.outR) A.outR[o] = BASE(rb) - val;
-    };
-    T accX[kMaxTasks][kRT], accU[kMaxTasks][kRT];
-    zeroAcc(accX);
-    zeroAcc(accU);
-    if (nonleaf) {
-        const bool qpl = D.costNl == kCostQuadraticPlusLinear;
-        const int sx = warp, su = slotFrom(warp, tasksOf(nx));  // x and u blocks on different warps
-        for (int jj = 0; jj < nc; jj++) {
-            const int r0 = jj * dIV;
-            const T *m = sMat + jj * perChild;
-            gemv(accX, m, nx, nx, sx, [&](int k) { return IN(r0 + k); });
-            gemv(accU, m + ldx * nx, nu, nu, su, [&](int k) { return IN(r0 + nx + k); });
-            if (qpl) {
-                const T d23 = T(-0.5) * (IN(r0 + nxu) + IN(r0 + nxu + 1));
-                gemv(accX, m + ldx * nx + ldu * nu, nx, 1, sx, [&](int) { return d23; });
-                gemv(accU, m + ldx * nx + ldu * nu + ldx, nu, 1, su, [&](int) { return d23; });
-            }
-        }
-#pragma unroll
-        for (int q = 0; q < kMaxTasks; q++) {
-            const int rx0 = (sx + q * kTileWarps) * kRT, ru0 = (su + q * kTileWarps) * kRT;
-#pragma unroll
-            for (int t = 0; t < kRT; t++) {
-                if (rx0 + t < nx) EMIT(rx0 + t, accX[q][t] + (rect ? IN(rIII + rx0 + t) : T(0)));
-                if (ru0 + t < nu) EMIT(nx + ru0 + t, accU[q][t] + (rect ? IN(rIII + nx + ru0 + t) : T(0)));
-            }
-        }
-        // y_i, the children's t and s, and the AVaR kernel projection (cache.cuh:650-676): entry
-        // k of the 4E+1 vector is formed by warp k % 8; in a T evaluation it goes to shared
-        // memory and each warp then applies rows of N N' to it
-        const T II = IN(rII);
-        auto avarOut = [&](int k) -> int {  // base row of entry k, -1 for padding
-            if (k < yD) return bY + k;
-            if (k < yD + D.ne) return k - yD < nc ? bT + (k - yD) : -1;
-            return k - yD - D.ne < nc ? bS + (k - yD - D.ne) : -1;
+    if (t0 < t1) prefetch(t0);
+    cpAsyncCommit();
+    for (int tile = t0; tile < t1; tile++) {
+        if (dbl && tile + 1 < t1) prefetch(tile + 1);
+        cpAsyncCommit();
+        cpAsyncWaitPrev(dbl);
+        __syncthreads();
+        const T *sIn = sBuf + (dbl ? ((tile - t0) & 1) * bufElems : 0), *sBase = sIn + nIn * inArr * kTileB;
+        const int b0 = tile * kTileB, b = b0 + lane;
+        const bool act = b < B;
+        auto IN = [&](int r) -> T {
+            T v = A.a1 * sIn[r * kTileB + lane];
+            if (inArr == 2) v += A.a2 * sIn[(nIn + r) * kTileB + lane];
+            return v;
         };
-        auto avarLin = [&](int k) -> T {  // the L* part of entry k
-            if (k < yD) return IN(rI + k) - P.b[(size_t)i * yD + k] * II;
-            if (k < yD + D.ne) {
-                const int jj = k - yD;
-                return T(0.5) * (IN(jj * dIV + nxu) + IN(jj * dIV + nxu + 1));
-            }
-            const int jj = k - yD - D.ne;
-            return (c0 + jj < D.nnl) ? IN(rS + 2 * jj) : T(0.5) * (IN(rS + 2 * jj) + IN(rS + 2 * jj + 1));
+        auto BASE = [&](int r) -> T {
+            if (!baseArr) return T(0);
+            T v = A.b1 * sBase[r * kTileB + lane];
+            if (baseArr == 2) v += A.b2 * sBase[(nBase + r) * kTileB + lane];
+            return v;
         };
-        if (MODE == 0) {
-            for (int k = warp; k < D.nd; k += kTileWarps) {
-                const int ob = avarOut(k);
-                sAv[k * kTileB + lane] = ob >= 0 ? BASE(ob) + A.cL * avarLin(k) : T(0);
+        auto EMIT = [&](int rb, T lv) {
+            if (!act) return;
+            const T bs = BASE(rb);
+            const size_t o = (size_t)rowBase(rb) * B + b;
+            if (A.outBase) A.outBase[o] = bs;
+            A.out[o] = bs + A.cL * lv;
+        };
+        auto FIN = [&](int rb, T val) {  // a final primal entry (mode 0) and its residual
+            if (!act) return;
+            const size_t o = (size_t)rowBase(rb) * B + b;
+            A.out[o] = val;
+            if (A.outR) A.outR[o] = BASE(rb) - val;
+        };
+        T accX[kMaxTasks][kRT], accU[kMaxTasks][kRT];
+        zeroAcc(accX);
+        zeroAcc(accU);
+        if (nonleaf) {
+            const bool qpl = D.costNl == kCostQuadraticPlusLinear;
+            const int sx = warp, su = slotFrom(warp, tasksOf(nx));  // x and u blocks on different warps
+            for (int jj = 0; jj < nc; jj++) {
+                const int r0 = jj * dIV;
+                const T *m = sMat + jj * perChild;
+                gemv(accX, m, nx, nx, sx, [&](int k) { return IN(r0 + k); });
+                gemv(accU, m + ldx * nx, nu, nu, su, [&](int k) { return IN(r0 + nx + k); });
+                if (qpl) {
+                    const T d23 = T(-0.5) * (IN(r0 + nxu) + IN(r0 + nxu + 1));
+                    gemv(accX, m + ldx * nx + ldu * nu, nx, 1, sx, [&](int) { return d23; });
+                    gemv(accU, m + ldx * nx + ldu * nu + ldx, nu, 1, su, [&](int) { return d23; });
+                }
             }
-            __syncthreads();
-            const T *N = P.NNtr + (size_t)i * D.nd * D.nd;
-            for (int k = warp; k < D.nd; k += kTileWarps) {
-                const int ob = avarOut(k);
-                if (ob < 0) continue;
-                T acc = 0;
-                for (int c = 0; c < D.nd; c++) acc += __ldg(N + (size_t)c * D.nd + k) * sAv[c * kTileB + lane];
-                FIN(ob, acc);
+    #pragma unroll
+            for (int q = 0; q < kMaxTasks; q++) {
+                const int rx0 = (sx + q * kTileWarps) * kRT, ru0 = (su + q * kTileWarps) * kRT;
+    #pragma unroll
+                for (int t = 0; t < kRT; t++) {
+                    if (rx0 + t < nx) EMIT(rx0 + t, accX[q][t] + (rect ? IN(rIII + rx0 + t) : T(0)));
+                    if (ru0 + t < nu) EMIT(nx + ru0 + t, accU[q][t] + (rect ? IN(rIII + nx + ru0 + t) : T(0)));
+                }
+            }
+            // y_i, the children's t and s, and the AVaR kernel projection (cache.cuh:650-676): entry
+            // k of the 4E+1 vector is formed by warp k % 8; in a T evaluation it goes to shared
+            // memory and each warp then applies rows of N N' to it
+            const T II = IN(rII);
+            auto avarOut = [&](int k) -> int {  // base row of entry k, -1 for padding
+                if (k < yD) return bY + k;
+                if (k < yD + D.ne) return k - yD < nc ? bT + (k - yD) : -1;
+                return k - yD - D.ne < nc ? bS + (k - yD - D.ne) : -1;
+            };
+            auto avarLin = [&](int k) -> T {  // the L* part of entry k
+                if (k < yD) return IN(rI + k) - P.b[(size_t)i * yD + k] * II;
+                if (k < yD + D.ne) {
+                    const int jj = k - yD;
+                    return T(0.5) * (IN(jj * dIV + nxu) + IN(jj * dIV + nxu + 1));
+                }
+                const int jj = k - yD - D.ne;
+                return (c0 + jj < D.nnl) ? IN(rS + 2 * jj) : T(0.5) * (IN(rS + 2 * jj) + IN(rS + 2 * jj + 1));
+            };
+            if (MODE == 0) {
+                for (int k = warp; k < D.nd; k += kTileWarps) {
+                    const int ob = avarOut(k);
+                    sAv[k * kTileB + lane] = ob >= 0 ? BASE(ob) + A.cL * avarLin(k) : T(0);
+                }
+                __syncthreads();
+                const T *N = P.NNtr + (size_t)i * D.nd * D.nd;
+                for (int k = warp; k < D.nd; k += kTileWarps) {
+                    const int ob = avarOut(k);
+                    if (ob < 0) continue;
+                    T acc = 0;
+                    for (int c = 0; c < D.nd; c++) acc += __ldg(N + (size_t)c * D.nd + k) * sAv[c * kTileB + lane];
+                    FIN(ob, acc);
+                }
+            } else {
+                for (int k = warp; k < D.nd; k += kTileWarps) {
+                    const int ob = avarOut(k);
+                    if (ob >= 0) EMIT(ob, avarLin(k));
+                }
+            }
+            if (warp == 0) {
+                if (i == 0) {  // t_0 carries no cost term; s_0 gets the prox of the objective
+                    if (MODE == 0) {
+                        FIN(bRoot, BASE(bRoot));
+                        FIN(bRoot + 1, BASE(bRoot + 1) + A.cL * II - P.step);
+                    } else {
+                        EMIT(bRoot, T(0));
+                        EMIT(bRoot + 1, II);
+                    }
+                }
             }
         } else {
-            for (int k = warp; k < D.nd; k += kTileWarps) {
-                const int ob = avarOut(k);
-                if (ob >= 0) EMIT(ob, avarLin(k));
+            gemv(accX, sMat, nx, nx, warp, [&](int k) { return IN(k); });
+            if (D.costL == kCostQuadraticPlusLinear) {
+                const T d23 = T(-0.5) * (IN(nx) + IN(nx + 1));
+                gemv(accX, sMat + ldx * nx, nx, 1, warp, [&](int) { return d23; });
             }
-        }
-        if (warp == 0) {
-            if (i == 0) {  // t_0 carries no cost term; s_0 gets the prox of the objective
-                if (MODE == 0) {
-                    FIN(bRoot, BASE(bRoot));
-                    FIN(bRoot + 1, BASE(bRoot + 1) + A.cL * II - P.step);
-                } else {
-                    EMIT(bRoot, T(0));
-                    EMIT(bRoot + 1, II);
+    #pragma unroll
+            for (int q = 0; q < kMaxTasks; q++) {
+                const int r0 = (warp + q * kTileWarps) * kRT;
+    #pragma unroll
+                for (int t = 0; t < kRT; t++) {
+                    const int r = r0 + t;
+                    if (r < nx) EMIT(r, accX[q][t] + (rect ? IN(dVI + r) : T(0)));
                 }
             }
         }
-    } else {
-        gemv(accX, sMat, nx, nx, warp, [&](int k) { return IN(k); });
-        if (D.costL == kCostQuadraticPlusLinear) {
-            const T d23 = T(-0.5) * (IN(nx) + IN(nx + 1));
-            gemv(accX, sMat + ldx * nx, nx, 1, warp, [&](int) { return d23; });
-        }
-#pragma unroll
-        for (int q = 0; q < kMaxTasks; q++) {
-            const int r0 = (warp + q * kTileWarps) * kRT;
-#pragma unroll
-            for (int t = 0; t < kRT; t++) {
-                const int r = r0 + t;
-                if (r < nx) EMIT(r, accX[q][t] + (rect ? IN(dVI + r) : T(0)));
-            }
-        }
+        __syncthreads();  // every warp is done with this tile's rows before the buffer is refilled
+        if (!dbl && tile + 1 < t1) prefetch(tile + 1);
     }
 }
 
@@ -331,12 +372,10 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem
 // ------------------------------------------------------------------------------------------
 template <typename T, int MODE>
 __global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T> P, const Dims D, const OpArgs<T> A,
-                                                              const PadMats<T> M) {
+                                                              const PadMats<T> M, int tilesPerCta, int dbl) {
     extern __shared__ __align__(16) unsigned char smraw[];
     T *sm = reinterpret_cast<T *>(smraw);
     const int B = D.B, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int b0 = blockIdx.x * kTileB, b = b0 + lane;
-    const bool act = b < B;
     const int j = blockIdx.y;
     const int nx = D.nx, nu = D.nu, nxu = D.nxu, dIV = D.dIV, dVI = D.dVI, yD = D.yD;
     const bool nonleaf = j < D.nnl;
@@ -378,187 +417,206 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T
     const int dSoc = dIV > dVI ? dIV : dVI;
     const int ldx = pad16(nx), ldu = pad16(nu);
     const int matIV = ldx * nx + ldu * nu, matElems = matIV + (nonleaf ? 0 : ldx * nx);
-    T *sMat = sm, *sw = sMat + matElems, *sPart = sw + dSoc * kTileB;
-    T *sIn = sPart + kTileWarps * kTileB, *sBase = sIn + nIn * inArr * kTileB;
+    const int bufElems = (nIn * inArr + nBase * baseArr) * kTileB;  // one tile's input and base rows
+    T *sMat = sm, *sw = sMat + matElems, *sPart = sw + dSoc * kTileB, *sBuf = sPart + kTileWarps * kTileB;
     if (j > 0) {
         stageMat(sMat, M.sqrtQ + (size_t)j * ldx * nx, ldx * nx);
         stageMat(sMat + ldx * nx, M.sqrtR + (size_t)j * ldu * nu, ldu * nu);
     }
     if (!nonleaf) stageMat(sMat + matIV, M.lSqrtQ, ldx * nx);
-    gather(sIn, nIn, A.in1, B, b0, lane, warp, rowIn);
-    if (A.in2) gather(sIn + nIn * kTileB, nIn, A.in2, B, b0, lane, warp, rowIn);
-    if (A.base1) gather(sBase, nBase, A.base1, B, b0, lane, warp, rowBase);
-    if (A.base2) gather(sBase + nBase * kTileB, nBase, A.base2, B, b0, lane, warp, rowBase);
-    cpAsyncWaitAll();
-    __syncthreads();
-    auto INP = [&](int r) -> T {
-        T v = A.a1 * sIn[r * kTileB + lane];
-        if (inArr == 2) v += A.a2 * sIn[(nIn + r) * kTileB + lane];
-        return v;
+    // This CTA's instance tiles [t0, t1), double-buffered as in k_lstar_b.
+    const int nTiles = (B + kTileB - 1) / kTileB;
+    const int t0 = blockIdx.x * tilesPerCta, t1 = min(t0 + tilesPerCta, nTiles);
+    auto prefetch = [&](int t) {
+        T *buf = sBuf + (dbl ? ((t - t0) & 1) * bufElems : 0);
+        const int bb = t * kTileB;
+        gather(buf, nIn, A.in1, B, bb, lane, warp, rowIn);
+        if (A.in2) gather(buf + nIn * kTileB, nIn, A.in2, B, bb, lane, warp, rowIn);
+        T *bs = buf + nIn * inArr * kTileB;
+        if (A.base1) gather(bs, nBase, A.base1, B, bb, lane, warp, rowBase);
+        if (A.base2) gather(bs + nBase * kTileB, nBase, A.base2, B, bb, lane, warp, rowBase);
     };
-    auto BASE = [&](int r) -> T {
-        if (!baseArr) return T(0);
-        T v = A.b1 * sBase[r * kTileB + lane];
-        if (baseArr == 2) v += A.b2 * sBase[(nBase + r) * kTileB + lane];
-        return v;
-    };
-    auto EMIT = [&](int rb, T lv) {
-        if (!act) return;
-        const T bs = BASE(rb);
-        const size_t o = (size_t)rowBase(rb) * B + b;
-        if (A.outBase) A.outBase[o] = bs;
-        A.out[o] = bs + A.cL * lv;
-    };
-    auto FIN = [&](int rb, T val) {  // a final dual entry (mode 0) and its residual
-        if (!act) return;
-        const size_t o = (size_t)rowBase(rb) * B + b;
-        A.out[o] = val;
-        if (A.outR) A.outR[o] = BASE(rb) - val;
-    };
-    // (v - proj(v)) * gamma for an SOC block staged in sw (dim rows), called by every warp after
-    // the barrier that publishes sw: the squared norm is summed over warps in shared memory
-    auto socBlock = [&](int dim, int rb0) {
-        T ss = 0;
-        for (int c = warp; c < dim - 1; c += kTileWarps) ss += sw[c * kTileB + lane] * sw[c * kTileB + lane];
-        sPart[warp * kTileB + lane] = ss;
+    if (t0 < t1) prefetch(t0);
+    cpAsyncCommit();
+    for (int tile = t0; tile < t1; tile++) {
+        if (dbl && tile + 1 < t1) prefetch(tile + 1);
+        cpAsyncCommit();
+        cpAsyncWaitPrev(dbl);
         __syncthreads();
-        ss = 0;
-#pragma unroll
-        for (int w = 0; w < kTileWarps; w++) ss += sPart[w * kTileB + lane];
-        const T nrm = sqrt(ss), tt = sw[(dim - 1) * kTileB + lane];
-        const int i1 = nrm <= tt, i2 = (nrm <= -tt) && !i1, i3 = !i1 && !i2;
-        const T sc = (nrm + tt) / (T(2) * nrm + T(1 - i3));
-        for (int c = warp; c < dim; c += kTileWarps) {
-            const T v = sw[c * kTileB + lane];
-            const T pr = i1 ? v : (i2 ? T(0) : (c < dim - 1 ? sc * v : sc * nrm));
-            FIN(rb0 + c, (v - pr) * g);
-        }
-    };
-    if (nonleaf) {
-        const int nm = 2 * P.numCh[j];
-        const int ry = rOwn, rs = rOwn + yD, rx = rs + 1, ru = rx + nx;
-        for (int k = warp; k < yD; k += kTileWarps) {
-            const T lv = INP(ry + k);
-            if (MODE == 0) {
-                const T v = (BASE(k) + A.cL * lv) * gi;
-                const T pr = (k < nm && v < T(0)) ? T(0) * v : v;  // AVaR dual cone (risks.cuh:99-106)
-                FIN(k, (v - pr) * g);
-            } else EMIT(k, lv);
-        }
-        if (warp == kTileWarps - 1) {
-            T lv = INP(rs);
-            for (int k = 0; k < yD; k++) lv -= __ldg(P.b + (size_t)j * yD + k) * INP(ry + k);
-            if (MODE == 0) {
-                const T v = (BASE(yD) + A.cL * lv) * gi;
-                FIN(yD, (v - (v > T(0) ? v : T(0))) * g);
-            } else EMIT(yD, lv);
-        }
-        if (rect)
-            for (int k = warp; k < nxu; k += kTileWarps) {
-                const T lv = k < nx ? INP(rx + k) : INP(ru + k - nx);
-                if (MODE == 0) {
-                    const T v = (BASE(bIII + k) + A.cL * lv) * gi;
-                    const T pr = boxProject(v, P.nlLo[(size_t)j * nxu + k], P.nlHi[(size_t)j * nxu + k]);
-                    FIN(bIII + k, (v - pr) * g);
-                } else EMIT(bIII + k, lv);
+        const T *sIn = sBuf + (dbl ? ((tile - t0) & 1) * bufElems : 0), *sBase = sIn + nIn * inArr * kTileB;
+        const int b0 = tile * kTileB, b = b0 + lane;
+        const bool act = b < B;
+        auto INP = [&](int r) -> T {
+            T v = A.a1 * sIn[r * kTileB + lane];
+            if (inArr == 2) v += A.a2 * sIn[(nIn + r) * kTileB + lane];
+            return v;
+        };
+        auto BASE = [&](int r) -> T {
+            if (!baseArr) return T(0);
+            T v = A.b1 * sBase[r * kTileB + lane];
+            if (baseArr == 2) v += A.b2 * sBase[(nBase + r) * kTileB + lane];
+            return v;
+        };
+        auto EMIT = [&](int rb, T lv) {
+            if (!act) return;
+            const T bs = BASE(rb);
+            const size_t o = (size_t)rowBase(rb) * B + b;
+            if (A.outBase) A.outBase[o] = bs;
+            A.out[o] = bs + A.cL * lv;
+        };
+        auto FIN = [&](int rb, T val) {  // a final dual entry (mode 0) and its residual
+            if (!act) return;
+            const size_t o = (size_t)rowBase(rb) * B + b;
+            A.out[o] = val;
+            if (A.outR) A.outR[o] = BASE(rb) - val;
+        };
+        // (v - proj(v)) * gamma for an SOC block staged in sw (dim rows), called by every warp after
+        // the barrier that publishes sw: the squared norm is summed over warps in shared memory
+        auto socBlock = [&](int dim, int rb0) {
+            T ss = 0;
+            for (int c = warp; c < dim - 1; c += kTileWarps) ss += sw[c * kTileB + lane] * sw[c * kTileB + lane];
+            sPart[warp * kTileB + lane] = ss;
+            __syncthreads();
+            ss = 0;
+    #pragma unroll
+            for (int w = 0; w < kTileWarps; w++) ss += sPart[w * kTileB + lane];
+            const T nrm = sqrt(ss), tt = sw[(dim - 1) * kTileB + lane];
+            const int i1 = nrm <= tt, i2 = (nrm <= -tt) && !i1, i3 = !i1 && !i2;
+            const T sc = (nrm + tt) / (T(2) * nrm + T(1 - i3));
+            for (int c = warp; c < dim; c += kTileWarps) {
+                const T v = sw[c * kTileB + lane];
+                const T pr = i1 ? v : (i2 ? T(0) : (c < dim - 1 ? sc * v : sc * nrm));
+                FIN(rb0 + c, (v - pr) * g);
             }
-    }
-    {  // IV_j = [sqrtQ_j x_a; sqrtR_j u_a; h; h] (costs.cuh:126-161, 379-417); zero at the root
-        T accX[kMaxTasks][kRT], accU[kMaxTasks][kRT];
-        zeroAcc(accX);
-        zeroAcc(accU);
-        T h = 0;
-        const int sx = warp, su = slotFrom(warp, tasksOf(nx));  // x and u blocks on different warps
-        if (j > 0) {
-            gemv(accX, sMat, nx, nx, sx, [&](int k) { return INP(k); });
-            gemv(accU, sMat + ldx * nx, nu, nu, su, [&](int k) { return INP(nx + k); });
-            h = T(0.5) * INP(nxu);
-            if (D.costNl == kCostQuadraticPlusLinear) {
+        };
+        if (nonleaf) {
+            const int nm = 2 * P.numCh[j];
+            const int ry = rOwn, rs = rOwn + yD, rx = rs + 1, ru = rx + nx;
+            for (int k = warp; k < yD; k += kTileWarps) {
+                const T lv = INP(ry + k);
+                if (MODE == 0) {
+                    const T v = (BASE(k) + A.cL * lv) * gi;
+                    const T pr = (k < nm && v < T(0)) ? T(0) * v : v;  // AVaR dual cone (risks.cuh:99-106)
+                    FIN(k, (v - pr) * g);
+                } else EMIT(k, lv);
+            }
+            if (warp == kTileWarps - 1) {
+                T lv = INP(rs);
+                for (int k = 0; k < yD; k++) lv -= __ldg(P.b + (size_t)j * yD + k) * INP(ry + k);
+                if (MODE == 0) {
+                    const T v = (BASE(yD) + A.cL * lv) * gi;
+                    FIN(yD, (v - (v > T(0) ? v : T(0))) * g);
+                } else EMIT(yD, lv);
+            }
+            if (rect)
+                for (int k = warp; k < nxu; k += kTileWarps) {
+                    const T lv = k < nx ? INP(rx + k) : INP(ru + k - nx);
+                    if (MODE == 0) {
+                        const T v = (BASE(bIII + k) + A.cL * lv) * gi;
+                        const T pr = boxProject(v, P.nlLo[(size_t)j * nxu + k], P.nlHi[(size_t)j * nxu + k]);
+                        FIN(bIII + k, (v - pr) * g);
+                    } else EMIT(bIII + k, lv);
+                }
+        }
+        {  // IV_j = [sqrtQ_j x_a; sqrtR_j u_a; h; h] (costs.cuh:126-161, 379-417); zero at the root
+            T accX[kMaxTasks][kRT], accU[kMaxTasks][kRT];
+            zeroAcc(accX);
+            zeroAcc(accU);
+            T h = 0;
+            const int sx = warp, su = slotFrom(warp, tasksOf(nx));  // x and u blocks on different warps
+            if (j > 0) {
+                gemv(accX, sMat, nx, nx, sx, [&](int k) { return INP(k); });
+                gemv(accU, sMat + ldx * nx, nu, nu, su, [&](int k) { return INP(nx + k); });
+                h = T(0.5) * INP(nxu);
+                if (D.costNl == kCostQuadraticPlusLinear) {
+                    T lin = 0;
+                    for (int k = 0; k < nx; k++) lin += __ldg(P.q + (size_t)j * nx + k) * INP(k);
+                    for (int k = 0; k < nu; k++) lin += __ldg(P.r + (size_t)j * nu + k) * INP(nx + k);
+                    h -= T(0.5) * lin;
+                }
+            }
+            if (MODE == 0) {
+    #pragma unroll
+                for (int q = 0; q < kMaxTasks; q++) {
+                    const int rx0 = (sx + q * kTileWarps) * kRT, ru0 = (su + q * kTileWarps) * kRT;
+    #pragma unroll
+                    for (int t = 0; t < kRT; t++) {
+                        const int r = rx0 + t, ru = ru0 + t;
+                        if (r < nx) sw[r * kTileB + lane] = (BASE(bIV + r) + A.cL * accX[q][t]) * gi + P.trans[(size_t)j * dIV + r];
+                        if (ru < nu)
+                            sw[(nx + ru) * kTileB + lane] =
+                                (BASE(bIV + nx + ru) + A.cL * accU[q][t]) * gi + P.trans[(size_t)j * dIV + nx + ru];
+                    }
+                }
+                if (warp == 0)
+                    for (int r = nxu; r < dIV; r++) sw[r * kTileB + lane] = (BASE(bIV + r) + A.cL * h) * gi + P.trans[(size_t)j * dIV + r];
+                __syncthreads();
+                socBlock(dIV, bIV);
+            } else {
+    #pragma unroll
+                for (int q = 0; q < kMaxTasks; q++) {
+                    const int rx0 = (sx + q * kTileWarps) * kRT, ru0 = (su + q * kTileWarps) * kRT;
+    #pragma unroll
+                    for (int t = 0; t < kRT; t++) {
+                        if (rx0 + t < nx) EMIT(bIV + rx0 + t, accX[q][t]);
+                        if (ru0 + t < nu) EMIT(bIV + nx + ru0 + t, accU[q][t]);
+                    }
+                }
+                if (warp == 0)
+                    for (int r = nxu; r < dIV; r++) EMIT(bIV + r, h);
+            }
+        }
+        if (!nonleaf) {  // V and VI of a leaf (constraints.cuh:168-170, costs.cuh:149-161/404-417)
+            const int rx = rOwn, rs = rOwn + nx;
+            if (rect)
+                for (int k = warp; k < nx; k += kTileWarps) {
+                    const T lv = INP(rx + k);
+                    if (MODE == 0) {
+                        const T v = (BASE(bV + k) + A.cL * lv) * gi;
+                        const T pr = boxProject(v, P.lLo[(size_t)l * nx + k], P.lHi[(size_t)l * nx + k]);
+                        FIN(bV + k, (v - pr) * g);
+                    } else EMIT(bV + k, lv);
+                }
+            T accX[kMaxTasks][kRT];
+            zeroAcc(accX);
+            gemv(accX, sMat + matIV, nx, nx, warp, [&](int k) { return INP(rx + k); });
+            T h = T(0.5) * INP(rs);
+            if (D.costL == kCostQuadraticPlusLinear) {
                 T lin = 0;
-                for (int k = 0; k < nx; k++) lin += __ldg(P.q + (size_t)j * nx + k) * INP(k);
-                for (int k = 0; k < nu; k++) lin += __ldg(P.r + (size_t)j * nu + k) * INP(nx + k);
+                for (int k = 0; k < nx; k++) lin += __ldg(P.lq + k) * INP(rx + k);
                 h -= T(0.5) * lin;
             }
-        }
-        if (MODE == 0) {
-#pragma unroll
-            for (int q = 0; q < kMaxTasks; q++) {
-                const int rx0 = (sx + q * kTileWarps) * kRT, ru0 = (su + q * kTileWarps) * kRT;
-#pragma unroll
-                for (int t = 0; t < kRT; t++) {
-                    const int r = rx0 + t, ru = ru0 + t;
-                    if (r < nx) sw[r * kTileB + lane] = (BASE(bIV + r) + A.cL * accX[q][t]) * gi + P.trans[(size_t)j * dIV + r];
-                    if (ru < nu)
-                        sw[(nx + ru) * kTileB + lane] =
-                            (BASE(bIV + nx + ru) + A.cL * accU[q][t]) * gi + P.trans[(size_t)j * dIV + nx + ru];
+            if (MODE == 0) {
+                __syncthreads();  // sw is reused after the IV block
+    #pragma unroll
+                for (int q = 0; q < kMaxTasks; q++) {
+                    const int r0 = (warp + q * kTileWarps) * kRT;
+    #pragma unroll
+                    for (int t = 0; t < kRT; t++) {
+                        const int r = r0 + t;
+                        if (r < nx) sw[r * kTileB + lane] = (BASE(bVI + r) + A.cL * accX[q][t]) * gi + P.lTrans[r];
+                    }
                 }
-            }
-            if (warp == 0)
-                for (int r = nxu; r < dIV; r++) sw[r * kTileB + lane] = (BASE(bIV + r) + A.cL * h) * gi + P.trans[(size_t)j * dIV + r];
-            __syncthreads();
-            socBlock(dIV, bIV);
-        } else {
-#pragma unroll
-            for (int q = 0; q < kMaxTasks; q++) {
-                const int rx0 = (sx + q * kTileWarps) * kRT, ru0 = (su + q * kTileWarps) * kRT;
-#pragma unroll
-                for (int t = 0; t < kRT; t++) {
-                    if (rx0 + t < nx) EMIT(bIV + rx0 + t, accX[q][t]);
-                    if (ru0 + t < nu) EMIT(bIV + nx + ru0 + t, accU[q][t]);
+                if (warp == 0)
+                    for (int r = nx; r < dVI; r++) sw[r * kTileB + lane] = (BASE(bVI + r) + A.cL * h) * gi + P.lTrans[r];
+                __syncthreads();
+                socBlock(dVI, bVI);
+            } else {
+    #pragma unroll
+                for (int q = 0; q < kMaxTasks; q++) {
+                    const int r0 = (warp + q * kTileWarps) * kRT;
+    #pragma unroll
+                    for (int t = 0; t < kRT; t++) {
+                        const int r = r0 + t;
+                        if (r < nx) EMIT(bVI + r, accX[q][t]);
+                    }
                 }
+                if (warp == 0)
+                    for (int r = nx; r < dVI; r++) EMIT(bVI + r, h);
             }
-            if (warp == 0)
-                for (int r = nxu; r < dIV; r++) EMIT(bIV + r, h);
         }
-    }
-    if (!nonleaf) {  // V and VI of a leaf (constraints.cuh:168-170, costs.cuh:149-161/404-417)
-        const int rx = rOwn, rs = rOwn + nx;
-        if (rect)
-            for (int k = warp; k < nx; k += kTileWarps) {
-                const T lv = INP(rx + k);
-                if (MODE == 0) {
-                    const T v = (BASE(bV + k) + A.cL * lv) * gi;
-                    const T pr = boxProject(v, P.lLo[(size_t)l * nx + k], P.lHi[(size_t)l * nx + k]);
-                    FIN(bV + k, (v - pr) * g);
-                } else EMIT(bV + k, lv);
-            }
-        T accX[kMaxTasks][kRT];
-        zeroAcc(accX);
-        gemv(accX, sMat + matIV, nx, nx, warp, [&](int k) { return INP(rx + k); });
-        T h = T(0.5) * INP(rs);
-        if (D.costL == kCostQuadraticPlusLinear) {
-            T lin = 0;
-            for (int k = 0; k < nx; k++) lin += __ldg(P.lq + k) * INP(rx + k);
-            h -= T(0.5) * lin;
-        }
-        if (MODE == 0) {
-            __syncthreads();  // sw is reused after the IV block
-#pragma unroll
-            for (int q = 0; q < kMaxTasks; q++) {
-                const int r0 = (warp + q * kTileWarps) * kRT;
-#pragma unroll
-                for (int t = 0; t < kRT; t++) {
-                    const int r = r0 + t;
-                    if (r < nx) sw[r * kTileB + lane] = (BASE(bVI + r) + A.cL * accX[q][t]) * gi + P.lTrans[r];
-                }
-            }
-            if (warp == 0)
-                for (int r = nx; r < dVI; r++) sw[r * kTileB + lane] = (BASE(bVI + r) + A.cL * h) * gi + P.lTrans[r];
-            __syncthreads();
-            socBlock(dVI, bVI);
-        } else {
-#pragma unroll
-            for (int q = 0; q < kMaxTasks; q++) {
-                const int r0 = (warp + q * kTileWarps) * kRT;
-#pragma unroll
-                for (int t = 0; t < kRT; t++) {
-                    const int r = r0 + t;
-                    if (r < nx) EMIT(bVI + r, accX[q][t]);
-                }
-            }
-            if (warp == 0)
-                for (int r = nx; r < dVI; r++) EMIT(bVI + r, h);
-        }
+        __syncthreads();  // every warp is done with this tile's rows (and sw) before they are refilled
+        if (!dbl && tile + 1 < t1) prefetch(tile + 1);
     }
 }
 

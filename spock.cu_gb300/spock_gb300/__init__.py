@@ -71,6 +71,9 @@ _SIGS = {
     "spock_kernel_time": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int, _dp, _lp]),
     "spock_round_time": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
     "spock_run_stats": (ctypes.c_int, [_vp, _lp, _lp]),
+    "spock_tuning": (ctypes.c_int, [_vp, _ip]),
+    "spock_resolve": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.c_long, _ip, _lp]),
+    "spock_resolve_device": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _ip, _lp]),
     "spock_project_dynamics_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
 }
 
@@ -258,6 +261,22 @@ class Cache:
         self._run(1, x0s, prev)
         return self._status.copy()
 
+    def resolveBatch(self, x0s, algo=0):
+        """Re-solve every instance warm-started from the current iterate (the previous solve's
+        solution, on the device) with new initial states.  Returns the status array."""
+        x0 = np.ascontiguousarray(np.atleast_2d(np.asarray(x0s, dtype=np.float64)))
+        if x0.shape[1] != self._tree.numStates():
+            raise ValueError("[initialiseState] wrong number of states")
+        _check(lib().spock_resolve(self._h, algo, _p(x0), x0.shape[0], self._status.ctypes.data_as(_ip),
+                                   self._iters.ctypes.data_as(_lp)))
+        return self._status.copy()
+
+    def resolveDevice(self, x0_device_ptr, algo=0):
+        """resolveBatch with the initial states on the device (as solveDevice)."""
+        _check(lib().spock_resolve_device(self._h, algo, ctypes.c_void_p(x0_device_ptr),
+                                          self._status.ctypes.data_as(_ip), self._iters.ctypes.data_as(_lp)))
+        return self._status.copy()
+
     def status(self, instance=0): return int(self._status[instance])
     def statuses(self): return self._status.copy()
     def solveIter(self, instance=0): return int(self._iters[instance])
@@ -340,6 +359,13 @@ class Cache:
         b = ctypes.c_long()
         _check(lib().spock_kernel_time(self._h, which.encode(), reps, ctypes.byref(ms), ctypes.byref(b)))
         return ms.value, b.value
+
+    def tuning(self):
+        """Tile shapes chosen by the autotuner for L* and L (runs it if needed)."""
+        out = np.zeros(5, dtype=np.int32)
+        _check(lib().spock_tuning(self._h, out.ctypes.data_as(_ip)))
+        return dict(zip(["lstar_tiles_per_cta", "lstar_double_buffer", "lop_tiles_per_cta", "lop_double_buffer",
+                         "batched_kernels"], out.tolist()))
 
     def runStats(self):
         """(rounds, kernel launches) of the last solve."""

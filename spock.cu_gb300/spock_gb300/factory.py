@@ -249,6 +249,7 @@ class Factory:
         self.l_con = NoConstraint()
         self.risk = None
         self.precondition = True
+        self.cost_scale = 1.
 
     def with_dynamics(self, d):
         self.dyn_events = [d] * (int(self.tree.events[1:].max()) + 1)
@@ -288,8 +289,37 @@ class Factory:
         self.precondition = enable
         return self
 
+    def with_cost_scaling(self, factor):
+        """Multiply every cost term (Q, R, q, r of the stage and leaf costs) by `factor` > 0.
+        Not in the reference factory.  The minimiser (x, u) is unchanged and the optimal value
+        is scaled by `factor`; the epigraph variables t, s and the risk variables y shrink with
+        it.  Chambolle-Pock takes one step size for the primal and the dual, so a cost-to-go
+        orders of magnitude above the state and dual magnitudes slows it down badly (nx = 50,
+        Q = diag U[1, 10] gives s_0 near 800); scaling the objective down balances them."""
+        if not factor > 0:
+            raise ValueError("cost scaling factor must be positive")
+        self.cost_scale = float(factor)
+        return self
+
     def generate_problem(self, path, dt="d", step_size=None):
+        if self.cost_scale != 1.:
+            import copy
+            f = copy.copy(self)
+            f.cost_events = [_scale_cost(c, self.cost_scale) for c in self.cost_events]
+            f.leaf_cost = _scale_cost(self.leaf_cost, self.cost_scale)
+            f.cost_scale = 1.
+            return Problem(f, path, dt, step_size)
         return Problem(self, path, dt, step_size)
+
+
+def _scale_cost(cost, factor):
+    import copy
+    c = copy.copy(cost)
+    for name in ("Q", "R", "q", "r"):
+        v = getattr(c, name, None)
+        if v is not None:
+            setattr(c, name, factor * np.asarray(v, float))
+    return c
 
 
 class Problem:
