@@ -1,10 +1,17 @@
-"""Benchmark: solves/sec to eps=1e-4 on one GB300, batched FP32 SPOCK vs plain FP64 SPOCK.
+"""Benchmark: solves/sec to eps=1e-4 on one GB300, batched warm-started FP32 SPOCK vs plain FP64 SPOCK.
 
-Workload (one "step"): the uniform batch of 1,024 instances that share the config-2 problem
-(3-state Markov chain, N=10, stopping stage 4 -> 607 nodes; nx=50, nu=20; quadratic-plus-linear
-costs, box constraints, AVaR(0.95)), each with its own x0 ~ U[-1,1]^50, solved by SuperMann
-(Anderson memory 5) to tol 1e-4 (absolute and relative, CacheBuilder::tol).  Synthetic data
-from fixed seeds; the per-instance vectors of the batch (11 GB) are far larger than L2.
+Workload: the uniform batch of 1,024 instances sharing the config-2 problem (3-state Markov
+chain, N=10, stopping stage 4 -> 607 nodes; nx=50, nu=20; quadratic-plus-linear costs Q=diag
+U[1,10], R=diag U[0.1,1], q, r ~ N(0,1); box |x|<=3, |u|<=1; AVaR(0.95)), with every cost term
+multiplied by 1e-3 (same minimiser; at the literal scale the cost-to-go is near 800 and SPOCK
+stalls near a residual of 1e-2 in FP64 as in FP32).  Each instance has its own x0 ~ U[-1,1]^50.
+
+One step is one receding-horizon re-solve of the whole batch: every x0 moves by a disturbance
+U[-0.05, 0.05]^50 (clipped to [-1, 1]) and every instance is re-solved by SuperMann (Anderson
+memory 5) to tol(1e-4) -- absolute and relative tolerance 1e-4, CacheBuilder::tol -- warm-started
+from its previous solution (the previousSolution path of cache.cuh:611-632), which stays on the
+device.  Before the warm-up steps the batch is solved once from a cold start (not timed).
+Synthetic data from fixed seeds; the batch's per-instance vectors (~10 GB) are far larger than L2.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -29,7 +36,7 @@ sys.path.insert(0, os.path.join(ROOT, "spock.cu_gb300"))
 
 METRIC = "solves/sec to eps=1e-4 on one GB300 (batched+warm-start FP32 vs plain FP64 SPOCK)"
 PROBLEM_DIR = os.environ.get("SPOCK_BENCH_DIR", "/tmp/spock_bench")
-TOL, ANDERSON = 1e-4, 5
+TOL, ANDERSON, COST_SCALE, DRIFT = 1e-4, 5, 1e-3, 0.05
 
 
 def parse():
@@ -41,6 +48,9 @@ def parse():
     ap.add_argument("--batch", type=int, default=1024)
     ap.add_argument("--max-iters", type=int, default=20000)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-fp64-baseline", action="store_true", help="skip the plain FP64 SPOCK solves on the GPU")
+    ap.add_argument("--measure", action="store_true",
+                    help="with --impl reference: full FP64 oracle re-solves, printing T evaluations per re-solve")
     return ap.parse_args()
 
 
@@ -49,17 +59,30 @@ def dist_info():
 
 
 def workload(seed, count, rank=0):
+    """Problem folder and this rank's initial states (instances rank*count .. (rank+1)*count-1)."""
     from spock_gb300 import configs
-    path, x0 = configs.cached("config2", PROBLEM_DIR + f"_r{rank}", seed=seed, count=count + 64 * rank)
-    return path, np.ascontiguousarray(x0[64 * rank:64 * rank + count])
+    path, x0 = configs.cached("config2", PROBLEM_DIR, seed=seed, count=count * (rank + 1), cost_scale=COST_SCALE)
+    return path, np.ascontiguousarray(x0[rank * count:(rank + 1) * count])
+
+
+def trajectory(x0s, steps, seed, rank=0):
+    """Initial states of the successive re-solves: x_k = clip(x_{k-1} + U[-0.05, 0.05], -1, 1)."""
+    rng = np.random.default_rng(1000003 * (seed + 1) + rank)
+    out, x = [], x0s.copy()
+    for _ in range(steps):
+        x = np.clip(x + rng.uniform(-DRIFT, DRIFT, x.shape), -1., 1.)
+        out.append(np.ascontiguousarray(x))
+    return out
 
 
 def config_dict(batch, world):
     return {"workload": "config4-uniform: %d instances of config2 (Markov 3 states, N=10, stopping 4, 607 nodes, "
-                        "nx=50, nu=20, quadratic-plus-linear costs, box |x|<=3 |u|<=1, AVaR 0.95), eps=1e-4, "
-                        "Anderson memory 5" % batch,
-            "instances_per_gpu": batch, "precision": "fp32 iteration, fp64 controller",
-            "l2": "inputs larger than L2 (per-step working set ~11 GB)", "parallelism": f"replicas x{world}"}
+                        "nx=50, nu=20, quadratic-plus-linear costs x 1e-3, box |x|<=3 |u|<=1, AVaR 0.95); step = "
+                        "warm-started re-solve of every instance after an x0 disturbance U[-0.05,0.05]^50, "
+                        "tol(1e-4), Anderson memory 5" % batch,
+            "instances_per_gpu": batch, "precision": "fp32 iteration, fp64 controller and reductions",
+            "cost_scale": COST_SCALE, "tolerance": "CacheBuilder::tol(1e-4): absolute and relative",
+            "l2": "inputs larger than L2 (per-step working set ~10 GB)", "parallelism": f"replicas x{world}"}
 
 
 class Clocks:
@@ -108,49 +131,85 @@ class Clocks:
 
 
 def cpu_sample(path, x0s, threads, iters):
-    """Oracle (FP64 C) on `threads` threads, each instance stopped after `iters` outer SPOCK
-    iterations; returns seconds per outer iteration per instance."""
+    """The oracle (FP64 C restatement of the reference iteration) on `threads` threads, one instance
+    each, stopped after `iters` outer SPOCK iterations.  Returns (seconds per T evaluation, wall
+    seconds): a T evaluation -- one CP step plus one M application -- is the unit of work every
+    SuperMann iteration spends one or more of."""
     from oracle import oracle
     oracle.build()
     P = oracle.Problem(path)
     opts = oracle.options(tol=TOL, anderson=ANDERSON, max_iters=iters)
-    secs, status, its, _, _ = P.solve_many(np.repeat(x0s[:1], threads, axis=0) if len(x0s) < threads else x0s[:threads],
-                                           opts, threads)
-    done = float(np.sum(np.maximum(its, 1)))
-    return secs * threads / done, secs
+    x = np.ascontiguousarray(np.resize(x0s, (threads, P.nx)))
+    zs = np.zeros((threads, P.size))
+    secs, status, its, calls, _ = P.solve_many_warm(x, zs, opts, threads, warm=False)
+    return secs * threads / float(np.sum(calls)), secs
 
 
-def measured_cpu_iterations():
-    """Outer iterations per config-2 solve measured by full oracle solves (committed summary)."""
+def committed_cpu_calls():
+    """T evaluations per warm re-solve measured by full FP64 oracle re-solves of this workload
+    (profiles/cpu_oracle_config2.md, written by `python bench.py --impl reference --measure`)."""
     fn = os.path.join(ROOT, "profiles", "cpu_oracle_config2.md")
     if os.path.exists(fn):
         for line in open(fn):
-            if line.startswith("mean_outer_iterations:"):
+            if line.startswith("mean_T_evaluations_per_resolve:"):
                 return float(line.split(":")[1])
     return None
+
+
+def measure_cpu_resolves(args):
+    """Full FP64 oracle re-solves of `threads` instances along the benchmark's x0 trajectory:
+    cold solve, then warm re-solves; prints the mean T evaluations and iterations per re-solve."""
+    from oracle import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    path, x0s = workload(args.seed, args.batch)
+    P = oracle.Problem(path)
+    n = min(threads, args.batch)
+    opts = oracle.options(tol=TOL, anderson=ANDERSON, max_iters=args.max_iters)
+    zs = np.zeros((n, P.size))
+    secs, st, its, calls, _ = P.solve_many_warm(x0s[:n], zs, opts, n, warm=False)
+    print(f"cold: {secs:.1f} s, converged {int((st == 0).sum())}/{n}, mean iterations {its.mean():.0f}, "
+          f"mean T evaluations {calls.mean():.0f}", flush=True)
+    rec_calls, rec_its = [], []
+    for k, x in enumerate(trajectory(x0s, args.warmup + args.steps, args.seed)):
+        secs, st, its, calls, _ = P.solve_many_warm(x[:n], zs, opts, n, warm=True)
+        print(f"re-solve {k}: {secs:.1f} s, converged {int((st == 0).sum())}/{n}, mean iterations {its.mean():.0f}, "
+              f"mean T evaluations {calls.mean():.0f}", flush=True)
+        if k >= args.warmup:
+            rec_calls.append(calls.mean())
+            rec_its.append(its.mean())
+    print(f"mean_T_evaluations_per_resolve: {np.mean(rec_calls):.1f}")
+    print(f"mean_outer_iterations_per_resolve: {np.mean(rec_its):.1f}")
+    print(f"instances: {n}, threads: {n}")
 
 
 def run_reference(args):
     rank, world, _ = dist_info()
     if rank != 0:
         return
+    if args.measure:
+        measure_cpu_resolves(args)
+        return
     threads = os.cpu_count() or 1
     path, x0s = workload(args.seed, max(threads, 1))
     iters = 25
-    per_iter = []
     for _ in range(args.warmup):
         cpu_sample(path, x0s, threads, iters)
-    t_total = 0.
+    per_call, t_total = [], 0.
     for _ in range(args.steps):
-        spi, secs = cpu_sample(path, x0s, threads, iters)
-        per_iter.append(spi)
+        spc, secs = cpu_sample(path, x0s, threads, iters)
+        per_call.append(spc)
         t_total += secs
-    spi = statistics.median(per_iter)
-    it_solve = measured_cpu_iterations() or float(args.max_iters)
-    value = threads / (spi * it_solve)
-    sample = (f"{threads} instances on {threads} threads, {iters} outer SPOCK iterations each per step; "
-              f"solves/s = threads / (s per outer iteration x {it_solve:.0f} outer iterations per solve, "
-              f"measured by full FP64 solves)")
+    spc = statistics.median(per_call)
+    calls = committed_cpu_calls()
+    if calls is None:
+        print(json.dumps({"impl": "reference", "unavailable": "profiles/cpu_oracle_config2.md (T evaluations per "
+                                                               "re-solve) is missing"}))
+        return
+    value = threads / (spc * calls)
+    sample = (f"{threads} instances on {threads} threads, {iters} outer SPOCK iterations each per step (FP64 C "
+              f"oracle); solves/s = threads / (s per T evaluation x {calls:.0f} T evaluations per warm re-solve, "
+              f"measured by full FP64 oracle re-solves of this workload)")
     out = {"metric": METRIC, "value": value, "unit": "solves/s", "impl": "reference", "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / max(args.steps, 1),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -158,6 +217,26 @@ def run_reference(args):
            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port", "sample": sample},
            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
+
+
+def fp64_cold_gpu(path, x0s, device, count, max_iters):
+    """Plain cold-started FP64 SPOCK on the same GPU, one instance at a time (the reference's usage,
+    examples/random/main.cu:41-70): solves/s over `count` solves."""
+    import spock_gb300 as sg
+    tree = sg.ScenarioTree(path)
+    data = sg.ProblemData(tree)
+    c = (sg.CacheBuilder(tree, data).tol(TOL).andersonBuffer(ANDERSON).maxIters(max_iters)
+         .precision(64).batch(1).device(device).build())
+    c.runSpock(x0s[0])  # warm-up: graph capture, autotuning
+    t0 = time.perf_counter()
+    st, its = [], []
+    for k in range(count):
+        c.reset()
+        st.append(c.runSpock(x0s[k]))
+        its.append(c.solveIter())
+    el = time.perf_counter() - t0
+    return {"value": count / el, "unit": "solves/s", "solves": count, "converged": int(sum(s == 0 for s in st)),
+            "outer_iterations_mean": float(np.mean(its)), "seconds": el}
 
 
 def run_gpu(args):
@@ -175,8 +254,9 @@ def run_gpu(args):
     data = sg.ProblemData(tree)
     cache = (sg.CacheBuilder(tree, data).tol(TOL).andersonBuffer(ANDERSON).maxIters(args.max_iters)
              .precision(32).batch(B).device(local).build())
-    nx = tree.numStates()
-    x0_dev = torch.tensor(x0s.T.copy(), dtype=torch.float32, device=f"cuda:{local}").contiguous()  # [nx][B]
+    nx, nu = tree.numStates(), tree.numInputs()
+    traj = trajectory(x0s, args.warmup + 2 * args.steps, args.seed, rank)
+    x_dev = [torch.tensor(x.T.copy(), dtype=torch.float32, device=f"cuda:{local}").contiguous() for x in traj]
 
     def barrier():
         if world > 1:
@@ -184,65 +264,59 @@ def run_gpu(args):
             dist.barrier()
         torch.cuda.synchronize()
 
-    def device_step():
-        st = cache.solveDevice(x0_dev.data_ptr())
-        return st
-
-    for _ in range(args.warmup):
-        torch.cuda.synchronize()
-        device_step()
+    cache.runSpockBatch(x0s)  # the cold solve the receding-horizon loop starts from (not timed)
+    cold_conv = int((cache.statuses() == 0).sum())
+    for k in range(args.warmup):
+        cache.resolveDevice(x_dev[k].data_ptr())
     clocks = Clocks(local)
     barrier()
     clocks.start()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t0 = time.perf_counter()
     e0.record()
-    statuses, iters, rounds, launches = [], [], 0, 0
-    for _ in range(args.steps):
-        st = device_step()
+    statuses, iters, calls, rounds, launches = [], [], [], 0, 0
+    for k in range(args.steps):
+        st = cache.resolveDevice(x_dev[args.warmup + k].data_ptr())
         statuses.append(st)
-        iters.append(cache.solveIters())
+        cnt = cache.countersAll()
+        iters.append(cnt[:, 6].copy())
+        calls.append(cnt[:, 5].copy())
         r, l = cache.runStats()
         rounds += r
         launches += l
     e1.record()
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
-    ms = e0.elapsed_time(e1)
     clk = clocks.stop()
-    t_dev = ms / 1e3
+    t_dev = e0.elapsed_time(e1) / 1e3
     if world > 1:
         import torch.distributed as dist
         tt = torch.tensor([t_dev])
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_dev = float(tt[0])
-    st_all = np.concatenate(statuses)
-    it_all = np.concatenate(iters)
+    st_all, it_all, calls_all = np.concatenate(statuses), np.concatenate(iters), np.concatenate(calls)
     conv = st_all == 0
     value = B * world * args.steps / t_dev
 
-    # end to end through the public API: host x0 in, statuses + first inputs out
+    # end to end through the public API: host x0 in (double), statuses + first inputs out
     barrier()
     t1 = time.perf_counter()
-    for _ in range(args.steps):
-        cache.runSpockBatch(x0s)
+    for k in range(args.steps):
+        cache.resolveBatch(traj[args.warmup + args.steps + k])
         u0 = cache.firstInputs()
     barrier()
     t_e2e = time.perf_counter() - t1
     e2e = {"value": B * world * args.steps / t_e2e, "unit": "solves/s",
-           "h2d_bytes_per_step": int(B * nx * 4), "d2h_bytes_per_step": int(B * (tree.numInputs() * 4 + 4 + 4))}
+           "h2d_bytes_per_step": int(B * nx * 8), "d2h_bytes_per_step": int(B * (nu * 8 + 4 + 8))}
 
-    # roofline of the dominant kernel: CUDA-event time of single launches on the engine stream
-    per_round = {}
+    # roofline of the dominant kernel: CUDA-event time of single launches on the solver stream
+    per_kernel = {}
     for k in ["lstar", "lop", "mlstar", "mlop", "dyn", "reduce", "update"]:
-        kms, kbytes = cache.kernelTime(k, 10)
-        per_round[k] = (kms, kbytes)
-    dom = max(per_round, key=lambda k: per_round[k][0])
-    kms, kbytes = per_round[dom]
-    peaks = {}
+        per_kernel[k] = cache.kernelTime(k, 10)
+    dom = max(per_kernel, key=lambda k: per_kernel[k][0])
+    kms, kbytes = per_kernel[dom]
     try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-        peak, peak_src = float(peaks["hbm_gbs"]), "measured"
+        peak, peak_src = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]), "measured"
     except (OSError, KeyError, ValueError):
         peak, peak_src = 6800., "fallback"
     achieved = kbytes / (kms / 1e3) / 1e9
@@ -250,32 +324,33 @@ def run_gpu(args):
     fn = os.path.join(ROOT, "profiles", "traffic.md")
     if os.path.exists(fn):
         for line in open(fn):
-            if line.startswith(f"{dom}_bytes_per_launch:"):
+            if line.startswith(f"{dom}_bytes_per_launch_b{B}:"):
                 traffic = float(line.split(":")[1])
 
-    cpu = None
+    out = None
     if rank == 0:
         threads = os.cpu_count() or 1
-        spi, _ = cpu_sample(path, x0s, threads, 25)
-        mean_it = float(np.mean(it_all[conv])) if conv.any() else float(args.max_iters)
-        cpu_val = threads / (spi * mean_it)
+        spc, _ = cpu_sample(path, x0s, threads, 25)
+        mean_calls = float(np.mean(calls_all))
+        cpu_val = threads / (spc * mean_calls)
         cpu = {"value": cpu_val, "unit": "solves/s", "cores": threads, "kind": "port",
-               "sample": f"{threads} instances x 25 outer SPOCK iterations (FP64 C oracle, {threads} threads); "
-                         f"extrapolated with the {mean_it:.0f} outer iterations per solve of this run"}
-    if rank == 0:
+               "sample": f"{threads} instances x 25 outer SPOCK iterations (FP64 C oracle, {threads} threads) -> s per "
+                         f"T evaluation, times the {mean_calls:.0f} T evaluations per re-solve of this run"}
+        fp64 = None if args.no_fp64_baseline else fp64_cold_gpu(path, x0s, local, 2, args.max_iters)
         out = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-               "config": config_dict(B, world),
-               "e2e": e2e,
-               "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
-                            "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                            "peak_source": peak_src, "kernel_ms": kms, "algorithmic_bytes": kbytes,
-                            "per_kernel_ms": {k: v[0] for k, v in per_round.items()}},
+               "config": config_dict(B, world), "e2e": e2e,
+               "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                            "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
+                            "kernel_ms": kms, "algorithmic_bytes": kbytes,
+                            "per_kernel_ms": {k: v[0] for k, v in per_kernel.items()},
+                            "per_kernel_gbs": {k: v[1] / v[0] / 1e6 for k, v in per_kernel.items()}},
                "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
-               "converged": int(conv.sum()), "instances": int(st_all.size),
+               "converged": int(conv.sum()), "instances": int(st_all.size), "cold_start_converged": cold_conv,
                "outer_iterations": {"mean": float(np.mean(it_all)), "max": int(np.max(it_all))},
-               "rounds_per_step": rounds / args.steps, "wall_s": wall}
+               "t_evaluations_mean": float(np.mean(calls_all)), "rounds_per_step": rounds / args.steps,
+               "tuning": cache.tuning(), "fp64_cold_single_gpu": fp64, "wall_s": wall}
         print(json.dumps(out))
     if world > 1:
         import torch.distributed as dist

@@ -65,6 +65,16 @@ int spock_problem_sizes(spock_problem p, long *sizes10);
 /* stepSize (problem.cuh:521) and the preconditioning scaling (nx+nu, ones if none). */
 int spock_problem_step(spock_problem p, double *step, double *scaling_or_null);
 
+/* The offline cache of the dynamics projection -- P, K, the lower Cholesky factors, (A+BK)' and
+ * (A+BK)'PB per node, which the reference computes in numpy when it generates a problem
+ * (api/python/spock/problem.py:192-213) -- recomputed on GPU `device` in FP64 from the problem's
+ * [A B] and tree.  Outputs (NULL skips one) use the layouts of the dynamics_P, _K, _lowCholesky,
+ * _ABKTr and _APB .bt files: nx*nx*numNodes, nu*nx*numNonleaf, nu*nu*numNonleaf, nx*nx*numNodes,
+ * nx*nu*numNodes doubles.  With replace != 0 the problem's cache is replaced by this one, so
+ * solvers created afterwards use it. */
+int spock_offline_dynamics(spock_problem p, int device, int replace, double *P, double *K, double *lowChol,
+                           double *ABKTr, double *APB);
+
 /* CacheBuilder<T>(tree, data)...build() (src/cache.cuh:1215-1244). */
 int spock_solver_create(spock_problem p, const spock_options *opts, spock_solver *out);
 void spock_solver_free(spock_solver s);
@@ -87,6 +97,12 @@ int spock_solve_device(spock_solver s, int algo, const void *x0_device, int *sta
 int spock_resolve(spock_solver s, int algo, const double *x0, long count, int *statuses, long *iters);
 int spock_resolve_device(spock_solver s, int algo, const void *x0_device, int *statuses, long *iters);
 
+/* Replace dst's iterate by src's, converted on the device to dst's precision: two solvers of the
+ * same problem and batch on the same GPU.  With src an FP32 solver and dst an FP64 one, a
+ * following spock_resolve(dst, ...) with the same initial states is the FP64 polish of the FP32
+ * solution (it continues from it under dst's tolerances).  No reference counterpart. */
+int spock_copy_iterate(spock_solver dst, spock_solver src);
+
 /* Results.  Cache::solution() (cache.cuh:378): the raw iterate of one instance, sizePrimal +
  * sizeDual doubles.  Cache::states()/inputs() (cache.cuh:386-412): unscaled, nx*numNodes and
  * nu*numNonleafNodes doubles.  first_inputs: the unscaled u_0 of every instance (batch*nu). */
@@ -99,6 +115,8 @@ int spock_status(spock_solver s, long instance, int *status, long *iters, double
 /* K0/K1/K2/backtracks/K3 counts, T evaluations and iterations of instance 0 (the debug
  * counters of cache.cuh:1101-1130). */
 int spock_counters(spock_solver s, long *out7);
+/* The same seven counters for every instance of the batch: batch x 7 values. */
+int spock_counters_all(spock_solver s, long *out_batch_by_7);
 /* reset() (cache.cuh:436-479): zero the iterate. */
 int spock_reset(spock_solver s);
 
@@ -117,9 +135,10 @@ int spock_round_time(spock_solver s, int rounds, double *ms);
 /* Rounds (one T evaluation + one M application per instance each) and kernel launches of the
  * last solve. */
 int spock_run_stats(spock_solver s, long *rounds, long *launches);
-/* Tile shapes the built-in autotuner chose for L* and L (it times 1, 2, 4 and 8 instance tiles
- * per CTA once, before the first solve): out5 = {L* tiles per CTA, L* double-buffered, L tiles
- * per CTA, L double-buffered, batched kernels in use}.  No reference counterpart. */
+/* Tile shapes the built-in autotuner chose (it times 1, 2, 4 and 8 instance tiles per CTA once,
+ * before the first solve): out5 = {L* tiles per CTA, L* double-buffered, L tiles per CTA, L
+ * double-buffered, dynamics-sweep tiles per CTA (0 when the small-batch kernels run)}.  No
+ * reference counterpart. */
 int spock_tuning(spock_solver s, int *out5);
 
 /* Dynamics projection that allocates no device memory.  No counterpart in the reference: it

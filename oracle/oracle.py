@@ -73,7 +73,7 @@ def lib():
                                     ctypes.c_int, _ip, _lp, _dp, _dp]
         L.or_solve_many_warm.restype = ctypes.c_double
         L.or_solve_many_warm.argtypes = [ctypes.c_void_p, ctypes.POINTER(OrOptions), ctypes.c_long, _dp,
-                                         ctypes.c_int, _ip, _lp, _dp, _dp, ctypes.c_int]
+                                         ctypes.c_int, _ip, _lp, _dp, _dp, ctypes.c_int, _lp]
         L.or_offline_dynamics.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp]
         L.or_offline_kernel.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_long, _dp]
         L.or_norm_L_sq.restype = ctypes.c_double
@@ -181,19 +181,21 @@ class Problem:
                                    _p(zs) if keep_z else None)
         return secs, status, iters, u0, zs
 
-    def solve_many_warm(self, x0s, zs, opts, threads):
-        """Solve each instance warm-started from its row of zs (count x size); zs is updated in
-        place with the solutions.  Returns (seconds, status, iters, u0)."""
+    def solve_many_warm(self, x0s, zs, opts, threads, warm=True):
+        """Solve each instance, warm-started from its row of zs (count x size) when `warm`; zs
+        receives the solutions.  Returns (seconds, status, iters, T calls, u0)."""
         x0s = np.ascontiguousarray(x0s, dtype=np.float64).reshape(-1, self.nx)
         cnt = x0s.shape[0]
         if zs.shape != (cnt, self.size) or zs.dtype != np.float64 or not zs.flags.c_contiguous:
             raise ValueError("zs must be a C-contiguous float64 array of shape (count, size)")
         status = np.zeros(cnt, dtype=np.int32)
         iters = np.zeros(cnt, dtype=np.int64)
+        calls = np.zeros(cnt, dtype=np.int64)
         u0 = np.zeros((cnt, self.nu))
         secs = lib().or_solve_many_warm(self.h, ctypes.byref(opts), cnt, _p(x0s), threads,
-                                        status.ctypes.data_as(_ip), iters.ctypes.data_as(_lp), _p(u0), _p(zs), 1)
-        return secs, status, iters, u0
+                                        status.ctypes.data_as(_ip), iters.ctypes.data_as(_lp), _p(u0), _p(zs),
+                                        int(warm), calls.ctypes.data_as(_lp))
+        return secs, status, iters, calls, u0
 
     def offline_dynamics(self, AB):
         AB = np.ascontiguousarray(AB, dtype=np.float64)

@@ -1012,6 +1012,7 @@ typedef struct {
     double *u0;
     double *zs;
     int warm;
+    long *calls;
 } Job;
 
 static void *job_run(void *arg) {
@@ -1024,6 +1025,7 @@ static void *job_run(void *arg) {
         or_run_spock(p, j->o, j->x0s + k * p->nx, z, j->warm, &st);
         j->status[k] = st.status;
         j->iters[k] = st.iters;
+        if (j->calls) j->calls[k] = st.calls_T;
         for (long q = 0; q < p->nu; q++) j->u0[k * p->nu + q] = z[q] / p->scaling[p->nx + q];
         if (j->zs) memcpy(j->zs + k * p->sZ, z, sizeof(double) * (size_t)p->sZ);
     }
@@ -1033,11 +1035,11 @@ static void *job_run(void *arg) {
 
 double or_solve_many(const OrProblem *p, const OrOptions *o, long count, const double *x0s, int threads,
                      int *status, long *iters, double *u0, double *zs) {
-    return or_solve_many_warm(p, o, count, x0s, threads, status, iters, u0, zs, 0);
+    return or_solve_many_warm(p, o, count, x0s, threads, status, iters, u0, zs, 0, NULL);
 }
 
 double or_solve_many_warm(const OrProblem *p, const OrOptions *o, long count, const double *x0s, int threads,
-                          int *status, long *iters, double *u0, double *zs, int warm) {
+                          int *status, long *iters, double *u0, double *zs, int warm, long *calls) {
     if (warm && !zs) return -1.;
     if (threads < 1) threads = 1;
     if (threads > count) threads = (int)count;
@@ -1047,7 +1049,7 @@ double or_solve_many_warm(const OrProblem *p, const OrOptions *o, long count, co
     const double t0 = now_s();
     for (int t = 0; t < threads; t++) {
         jobs[t].p = p; jobs[t].o = o; jobs[t].x0s = x0s; jobs[t].status = status; jobs[t].iters = iters;
-        jobs[t].u0 = u0; jobs[t].zs = zs; jobs[t].warm = warm;
+        jobs[t].u0 = u0; jobs[t].zs = zs; jobs[t].warm = warm; jobs[t].calls = calls;
         jobs[t].begin = count * t / threads;
         jobs[t].end = count * (t + 1) / threads;
         pthread_create(&th[t], NULL, job_run, &jobs[t]);

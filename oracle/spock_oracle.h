@@ -75,9 +75,11 @@ void or_states_inputs(const OrProblem *p, const double *z, double *states, doubl
 double or_solve_many(const OrProblem *p, const OrOptions *o, long count, const double *x0s,
                      int threads, int *status, long *iters, double *u0, double *zs_or_null);
 /* Same; with warm != 0 each instance starts from its iterate in zs (count*sZ, required) -- the
- * previousSolution warm start of cache.cuh:611-632 -- and zs receives the solutions. */
+ * previousSolution warm start of cache.cuh:611-632 -- and zs receives the solutions.  calls, if
+ * not NULL, receives each instance's number of T evaluations. */
 double or_solve_many_warm(const OrProblem *p, const OrOptions *o, long count, const double *x0s,
-                          int threads, int *status, long *iters, double *u0, double *zs, int warm);
+                          int threads, int *status, long *iters, double *u0, double *zs, int warm,
+                          long *calls);
 
 /* Offline dynamics cache (problem.py:192-213) from per-node [A B] (nx x (nx+nu) x n):
  * writes P (nx*nx*n), K (nu*nx*nnl), lowChol (nu*nu*nnl), ABKTr (nx*nx*n), APB (nx*nu*n). */

@@ -9,6 +9,7 @@
 
 #include "capi_internal.hpp"
 #include "engine.cuh"
+#include "offline.hpp"
 #include "problem.hpp"
 
 struct spock_problem_s {
@@ -161,6 +162,38 @@ int spock_solve_device(spock_solver sv, int algo, const void *x0, int *statuses,
     });
 }
 
+int spock_offline_dynamics(spock_problem pp, int device, int replace, double *P, double *K, double *lowChol,
+                           double *ABKTr, double *APB) {
+    return guard([&] {
+        need(pp, "problem");
+        spock::HostProblem &hp = pp->hp;
+        spock::OfflineCache c = spock::offlineDynamicsGpu(hp, device);
+        auto put = [](const std::vector<double> &v, double *out) {
+            if (out) std::memcpy(out, v.data(), sizeof(double) * v.size());
+        };
+        put(c.P, P);
+        put(c.K, K);
+        put(c.lowChol, lowChol);
+        put(c.ABKTr, ABKTr);
+        put(c.APB, APB);
+        if (replace) {
+            hp.P = c.P;
+            hp.K = c.K;
+            hp.lowChol = c.lowChol;
+            hp.ABKTr = c.ABKTr;
+            hp.APB = c.APB;
+            if (hp.affine) {  // Pe = P e per node (dynamics.cuh:236)
+                const long n = hp.numNodes, nx = hp.nx;
+                hp.Pe.assign((size_t)(nx * n), 0.);
+                for (long j = 0; j < n; j++)
+                    for (long col = 0; col < nx; col++)
+                        for (long r = 0; r < nx; r++)
+                            hp.Pe[j * nx + r] += hp.P[j * nx * nx + col * nx + r] * hp.e[j * nx + col];
+            }
+        }
+    });
+}
+
 int spock_resolve(spock_solver sv, int algo, const double *x0, long count, int *statuses, long *iters) {
     return guard([&] {
         auto *s = solver(sv);
@@ -180,6 +213,16 @@ int spock_resolve_device(spock_solver sv, int algo, const void *x0, int *statuse
         s->eng->setInitialStatesDevice(x0, s->eng->batch());
         s->eng->run(algo == SPOCK_ALGO_SPOCK ? spock::kSpock : spock::kCp, true);
         finishSolve(s, statuses, iters);
+    });
+}
+
+int spock_copy_iterate(spock_solver dst, spock_solver src) {
+    return guard([&] {
+        auto *d = solver(dst);
+        auto *s = solver(src);
+        // the source's stream has finished: every solve and setter synchronizes before returning
+        d->eng->setIterateFromDevice(s->eng->iterateDevice(), s->eng->precisionBits(),
+                                     s->eng->problem().sizeIterate(), s->eng->batch(), s->eng->device());
     });
 }
 
@@ -237,6 +280,14 @@ int spock_counters(spock_solver sv, long *out7) {
         auto *s = solver(sv);
         need(out7, "out");
         s->eng->getCounters(out7);
+    });
+}
+
+int spock_counters_all(spock_solver sv, long *out) {
+    return guard([&] {
+        auto *s = solver(sv);
+        need(out, "out");
+        s->eng->getCountersAll(out);
     });
 }
 

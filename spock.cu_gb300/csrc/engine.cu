@@ -335,10 +335,87 @@ __global__ void __launch_bounds__(256) k_update(const Dims Dm, const UpdArgs<T> 
     }
 }
 
+// The same update for batches of >= 32 instances, one thread per (instance, row subset): lane b
+// reads its action once and streams rows k of a chunk with stride 8 (the warps of the block), so
+// every warp access is one 128-byte row segment of 32 instances, with no per-element index
+// arithmetic or branch.
+template <typename T>
+__global__ void __launch_bounds__(256) k_update_b(const Dims Dm, const UpdArgs<T> A, long rowsPerChunk) {
+    const int B = Dm.B;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int b = blockIdx.x * 32 + lane;
+    if (b >= B) return;
+    const long k0 = (long)blockIdx.y * rowsPerChunk;
+    const long k1 = k0 + rowsPerChunk < Dm.sZ ? k0 + rowsPerChunk : Dm.sZ;
+    const size_t slot = (size_t)Dm.sZ * B;
+    switch (A.action[b]) {
+        case kActAK0:
+        case kActALs: {
+            const int m = A.m;
+            const int h = (A.head[b] + m - 1) % m;  // slot written this round (head already advanced)
+            const bool useAnd = A.useAnd[b];
+            T g[kMaxAnderson];
+#pragma unroll
+            for (int s2 = 0; s2 < kMaxAnderson; s2++)
+                g[s2] = (useAnd && s2 < m) ? T(A.gamma[(size_t)b * kMaxAnderson + s2]) : T(0);
+            for (long k = k0 + warp; k < k1; k += 8) {
+                const size_t o = (size_t)k * B + b;
+                const T z = A.Z[o], r = A.R[o], c = A.CAND[o];
+                const T dr = r - A.RPREV[o];
+                const T dzr = (z - A.PREV[o]) - dr;
+                T d = -r;
+                if (useAnd)
+#pragma unroll
+                    for (int s2 = 0; s2 < kMaxAnderson; s2++)
+                        if (s2 < m) d -= g[s2] * (s2 == h ? dzr : A.ANDZ[s2 * slot + o]);
+                A.ANDR[h * slot + o] = dr;
+                A.ANDZ[h * slot + o] = dzr;
+                A.D[o] = d;
+                A.PREV[o] = z;
+                A.RPREV[o] = r;
+                A.BACKUP[o] = c;
+                A.Z[o] = z + d;
+            }
+            break;
+        }
+        case kActFinish:
+        case kActCp:
+            for (long k = k0 + warp; k < k1; k += 8) A.Z[(size_t)k * B + b] = A.CAND[(size_t)k * B + b];
+            break;
+        case kActBK2: {
+            const T cf = T(A.coef[b]);
+            for (long k = k0 + warp; k < k1; k += 8) {
+                const size_t o = (size_t)k * B + b;
+                A.Z[o] = A.PREV[o] - cf * A.R[o];
+            }
+            break;
+        }
+        case kActBK3:
+            for (long k = k0 + warp; k < k1; k += 8) A.Z[(size_t)k * B + b] = A.BACKUP[(size_t)k * B + b];
+            break;
+        case kActBBt: {
+            const T tau = T(A.tau[b]);
+            for (long k = k0 + warp; k < k1; k += 8) {
+                const size_t o = (size_t)k * B + b;
+                A.Z[o] = A.PREV[o] + tau * A.D[o];
+            }
+            break;
+        }
+        default:
+            break;
+    }
+}
+
 // ------------------------------------------------------------------------------------------ small kernels
 template <typename T>
 __global__ void k_fill(T *p, size_t n, T v) {
     for (size_t o = (size_t)blockIdx.x * blockDim.x + threadIdx.x; o < n; o += (size_t)gridDim.x * blockDim.x) p[o] = v;
+}
+
+template <typename D, typename S>
+__global__ void k_convert(D *dst, const S *src, size_t n) {
+    for (size_t o = (size_t)blockIdx.x * blockDim.x + threadIdx.x; o < n; o += (size_t)gridDim.x * blockDim.x)
+        dst[o] = (D)src[o];
 }
 
 template <typename T>
@@ -378,6 +455,14 @@ __global__ void k_force_phaseA(DevState S, int B, int m) {
     S.head[b] = 1 % m;
 }
 
+// Convergence mask of the node kernels: tile t (instances 32t .. 32t+31) stays live while one
+// of its instances is running; the batched kernels skip the others.
+__global__ void k_tile_flags(const int *status, int B, int *tileLive) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned any = __ballot_sync(0xffffffffu, b < B && status[b] == -1);
+    if ((threadIdx.x & 31) == 0 && b < B) tileLive[b >> 5] = any != 0;
+}
+
 __global__ void k_count_active(const int *status, int B, int *out) {
     __shared__ int cnt;
     if (threadIdx.x == 0) cnt = 0;
@@ -401,11 +486,6 @@ public:
         if (batch < 1) throw std::invalid_argument("[Cache] batch must be >= 1");
         if (opt.anderson < 1 || opt.anderson > kMaxAnderson)
             throw std::invalid_argument("[Cache] Anderson buffer must be in [1, " + std::to_string(kMaxAnderson) + "]");
-        if (hp.costNonleaf == kCostLinear || hp.costLeaf == kCostLinear)
-            throw std::invalid_argument("[Cache] linear costs are not supported by the GB300 kernels yet");
-        if ((hp.conNonleaf != kConNone && hp.conNonleaf != kConRectangle) ||
-            (hp.conLeaf != kConNone && hp.conLeaf != kConRectangle))
-            throw std::invalid_argument("[Cache] polyhedral constraints are not supported by the GB300 kernels yet");
         CK(cudaSetDevice(device));
         CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
         buildDims();
@@ -452,6 +532,20 @@ public:
         CK(cudaStreamSynchronize(stream_));
     }
 
+    const void *iterateDevice() const override { return Z_; }
+
+    void setIterateFromDevice(const void *src, int srcBits, long sZ, long batch, int srcDevice) override {
+        if (sZ != D_.sZ || batch != B_)
+            throw std::invalid_argument("[copyIterate] solvers differ in problem size or batch");
+        if (srcDevice != device_) throw std::invalid_argument("[copyIterate] solvers are on different devices");
+        const size_t n = (size_t)D_.sZ * B_;
+        const int grid = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+        if (srcBits == 64) k_convert<T, double><<<grid, 256, 0, stream_>>>(Z_, (const double *)src, n);
+        else k_convert<T, float><<<grid, 256, 0, stream_>>>(Z_, (const float *)src, n);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(stream_));
+    }
+
     void zeroIterate() override {
         fill(Z_, (size_t)D_.sZ * B_, T(0));
     }
@@ -473,8 +567,9 @@ public:
         }
         k_init_state<<<((int)B_ + 127) / 128, 128, 0, stream_>>>(S_, (int)B_, warm ? 1 : 0);
         CK(cudaGetLastError());
+        allLive();
         int rounds = 0, polls = 0;
-        long launches = (algo == kSpock ? 5 : 2) + 1;  // buffer fills + state init
+        long launches = (algo == kSpock ? 5 : 2) + 2;  // buffer fills + state init + tile flags
         const int poll = B_ > 1 ? 10 : 25;
         if (algo == kSpock) {
             ensureGraph();
@@ -495,8 +590,9 @@ public:
                 reduceLaunch(kCp, check);
                 controlLaunch(kCp);
                 updateLaunch();
+                tileFlagsLaunch();
                 rounds++;
-                launches += (D_.ns - 1) * 2 + 2 + (check ? 3 : 2) + 1;
+                launches += (D_.ns - 1) * 2 + 2 + (check ? 3 : 2) + 2;
                 if (rounds % poll == 0) {
                     polls++;
                     if (activeCount(t0) == 0) break;
@@ -555,7 +651,18 @@ public:
         }
     }
 
+    void getCountersAll(long *out) override {
+        int *ptrs[7] = {S_.k0, S_.k1, S_.k2, S_.k2bt, S_.k3, S_.calls, S_.iters};
+        std::vector<int> h((size_t)B_);
+        for (int k = 0; k < 7; k++) {
+            CK(cudaMemcpyAsync(h.data(), ptrs[k], sizeof(int) * (size_t)B_, cudaMemcpyDeviceToHost, stream_));
+            CK(cudaStreamSynchronize(stream_));
+            for (long b = 0; b < B_; b++) out[(size_t)b * 7 + k] = h[(size_t)b];
+        }
+    }
+
     void op(const double *prim, double *dual) override {
+        allLive();
         uploadSlice(W1_, prim, 0, D_.sPrim);
         OpArgs<T> A = blankArgs();
         A.in1 = W1_; A.a1 = 1; A.cL = 1; A.out = W2_;
@@ -564,6 +671,7 @@ public:
     }
 
     void adj(const double *dual, double *prim) override {
+        allLive();
         uploadSlice(W1_, dual, D_.sPrim, D_.sDual);
         OpArgs<T> A = blankArgs();
         A.in1 = W1_; A.a1 = 1; A.cL = 1; A.out = W2_;
@@ -572,6 +680,7 @@ public:
     }
 
     void cpStep(const double *x0, const double *z, double *cand) override {
+        allLive();
         setInitialStates(x0, 1);
         uploadSlice(Z_, z, 0, D_.sZ);
         teval();
@@ -579,6 +688,7 @@ public:
     }
 
     void applyM(const double *z, double *mz) override {
+        allLive();
         // M z through the residual kernels, which read the residual buffer
         uploadSlice(R_, z, 0, D_.sZ);
         applyMres();
@@ -587,11 +697,12 @@ public:
 
     void tuning(int *out5) override {
         autotune();
-        out5[0] = tpcLstar_; out5[1] = lstarDbl_; out5[2] = tpcLop_; out5[3] = lopDbl_; out5[4] = batched_;
+        out5[0] = tpcLstar_; out5[1] = lstarDbl_; out5[2] = tpcLop_; out5[3] = lopDbl_; out5[4] = batched_ ? tpcDyn_ : 0;
     }
 
     double kernelMs(const char *which, int reps) override {
         autotune();
+        allLive();  // time the kernels over the whole batch
         cudaEvent_t e0, e1;
         CK(cudaEventCreate(&e0));
         CK(cudaEventCreate(&e1));
@@ -686,7 +797,7 @@ public:
         CK(cudaStreamSynchronize(stream));
     }
 
-    int launchesPerRound() const override { return 2 * (D_.ns - 1) + 2 + 2 + 3; }
+    int launchesPerRound() const override { return 2 * (D_.ns - 1) + 2 + 2 + 4; }
 
 private:
     Options opt_;
@@ -696,6 +807,8 @@ private:
     bool batched_ = false;  // kernels_batch.cuh for >= 32 instances, kernels.cuh otherwise
     bool lstarDbl_ = false, lopDbl_ = false;  // L*, L double-buffer their instance tiles
     int tpcLstar_ = 1, tpcLop_ = 1;           // instance tiles per L* / L CTA (autotune())
+    int tpcDyn_ = 1;                          // instance tiles per dynamics-sweep CTA
+    bool backDbl_ = false, fwdDbl_ = false;
     bool tuned_ = false;
     static constexpr int kTilesPerCta = 8;
     DevState S_{};
@@ -749,6 +862,7 @@ private:
         D.costNl = p.costNonleaf; D.costL = p.costLeaf; D.conNl = p.conNonleaf; D.conL = p.conLeaf;
         D.affine = p.affine ? 1 : 0;
         D.dIII = (int)p.dimIII; D.dIV = (int)p.dimIV; D.dV = (int)p.dimV; D.dVI = (int)p.dimVI;
+        D.gNl = (int)p.nlGammaRows; D.gL = (int)p.lGammaRows;
         D.oX = p.sizeU; D.oY = D.oX + p.sizeX; D.oT = D.oY + p.sizeY; D.oS = D.oT + p.sizeT; D.sPrim = p.sizePrim;
         D.oI = p.sizePrim; D.oII = D.oI + p.sizeI; D.oIII = D.oII + p.sizeII; D.oIV = D.oIII + p.sizeIII;
         D.oV = D.oIV + p.sizeIV; D.oVI = D.oV + p.sizeV; D.sDual = p.sizeDual; D.sZ = p.sizeIterate();
@@ -773,6 +887,7 @@ private:
         P_.lSqrtQ = upvec<T>(p.leafSqrtQ); P_.lq = upvec<T>(p.leafQ); P_.lTrans = upvec<T>(p.leafTranslation);
         P_.nlLo = upvec<T>(p.nlLower); P_.nlHi = upvec<T>(p.nlUpper); P_.lLo = upvec<T>(p.lLower); P_.lHi = upvec<T>(p.lUpper);
         P_.NNtr = upvec<T>(p.NNtr); P_.b = upvec<T>(p.b);
+        P_.grad = upvec<T>(p.gradient); P_.lGrad = upvec<T>(p.leafGradient);
         P_.step = (T)p.stepSize;
         scal_ = const_cast<T *>(upvec<T>(p.scaling));
     }
@@ -800,36 +915,57 @@ private:
     size_t lu() const { return (size_t)pad16(D_.nu); }
     // L* and L stage the node's matrices once and one (or, double-buffered, two) instance
     // tiles of input and base rows.
+    // rows of the constraint blocks: identity part and Gamma part (nonleaf, leaf)
+    int idNl() const { return (D_.conNl == kConRectangle || D_.conNl == kConPolyhedronWithIdentity) ? D_.nxu : 0; }
+    int idL() const { return (D_.conL == kConRectangle || D_.conL == kConPolyhedronWithIdentity) ? D_.nx : 0; }
+    int gNl() const { return (D_.conNl == kConPolyhedron || D_.conNl == kConPolyhedronWithIdentity) ? D_.gNl : 0; }
+    int gL() const { return (D_.conL == kConPolyhedron || D_.conL == kConPolyhedronWithIdentity) ? D_.gL : 0; }
+    bool needsBatched() const {
+        return D_.costNl == kCostLinear || D_.costL == kCostLinear || gNl() > 0 || gL() > 0 ||
+               D_.conNl == kConPolyhedronWithIdentity || D_.conL == kConPolyhedronWithIdentity;
+    }
     size_t bLstar(bool dbl = false) const {
-        const size_t in = (size_t)std::max(D_.ne * D_.dIV + D_.nxu + D_.yD + 1 + 2 * D_.ne, D_.dVI + D_.nx);
+        const size_t in = (size_t)std::max(D_.ne * D_.dIV + idNl() + gNl() + D_.yD + 2 + 2 * D_.ne, D_.dVI + idL() + gL());
         const size_t base = (size_t)std::max(D_.nxu + D_.yD + 2 * D_.ne + 2, D_.nx);
-        const size_t mats = std::max((size_t)D_.ne * (lx() * D_.nx + lu() * D_.nu + lx() + lu()), lx() * D_.nx + lx());
-        return (mats + ((dbl ? 2 : 1) * (in + base) + (size_t)D_.nd) * kTileB) * sizeof(T);
+        const size_t mats = std::max((size_t)D_.ne * (lx() * D_.nx + lu() * D_.nu + lx() + lu()), lx() * D_.nx + lx()) +
+                            std::max((size_t)pad16(D_.nxu) * gNl(), (size_t)pad16(D_.nx) * gL());
+        const size_t gv = (gNl() || gL()) ? (size_t)D_.nxu : 0;
+        return (mats + ((dbl ? 2 : 1) * (in + base) + (size_t)D_.nd + gv) * kTileB) * sizeof(T) + (in + base) * sizeof(int);
     }
     size_t bLop(bool dbl = false) const {
         const size_t in = (size_t)std::max(2 * D_.nxu + D_.yD + 2, D_.nxu + D_.nx + 2);
-        const size_t base = (size_t)std::max(D_.yD + 1 + D_.nxu + D_.dIV, D_.dIV + D_.nx + D_.dVI);
-        const size_t mats = 2 * lx() * D_.nx + lu() * D_.nu;
+        const size_t base = (size_t)std::max(D_.yD + 1 + idNl() + gNl() + D_.dIV, D_.dIV + idL() + gL() + D_.dVI);
+        const size_t mats = 2 * lx() * D_.nx + lu() * D_.nu +
+                            std::max((size_t)pad16(gNl()) * D_.nxu, (size_t)pad16(gL()) * D_.nx);
         return (mats + ((size_t)std::max(D_.dIV, D_.dVI) + kTileWarps + (dbl ? 2 : 1) * (2 * in + base)) * kTileB) *
-               sizeof(T);
+                   sizeof(T) +
+               (in + base) * sizeof(int);
     }
     size_t smLstarB() const { return bLstar(lstarDbl_); }
     size_t smLopB() const { return bLop(lopDbl_); }
     bool canDblLstar() const { return bLstar(true) <= 220 * 1024; }
     bool canDblLop() const { return bLop(true) <= 220 * 1024; }
-    size_t bBack() const {
+    size_t bBack(bool dbl = false) const {
         const size_t mats = (size_t)D_.ne * (lu() * D_.nx + lx() * D_.nu + lx() * D_.nx) + lx() * D_.nu + lu() * D_.nu;
-        return (mats + (size_t)(D_.ne * D_.nx + 2 * D_.nu + D_.nx) * kTileB) * sizeof(T);
+        return (mats + ((dbl ? 2 : 1) * (size_t)(D_.ne * D_.nx + D_.nu + D_.nx) + D_.nu) * kTileB) * sizeof(T);
     }
-    size_t bFwd() const {
+    size_t bFwd(bool dbl = false) const {
         const size_t mats = lu() * D_.nx + (size_t)D_.ne * lx() * D_.nxu;
-        return (mats + (size_t)(D_.nxu + 2 * D_.nu + D_.ne * D_.nx + D_.nx) * kTileB) * sizeof(T);
+        return (mats + (dbl ? 2 : 1) * (size_t)(D_.nxu + 2 * D_.nu + D_.ne * D_.nx + D_.nx) * kTileB) * sizeof(T);
     }
+    bool canDblBack() const { return bBack(true) <= 220 * 1024; }
+    bool canDblFwd() const { return bFwd(true) <= 220 * 1024; }
 
     void chooseKernels() {
         const int maxRows = kRT * kTileWarps * kMaxTasks;
-        batched_ = B_ >= kTileB && pad16(D_.nx) <= maxRows && pad16(D_.nu) <= maxRows && D_.nd <= 64 &&
-                   std::max({bLstar(), bLop(), bBack(), bFwd()}) <= 220 * 1024;
+        // linear costs and polyhedral constraints exist only in the batched kernels, which also run
+        // batches below one tile (the lanes past the batch stay idle)
+        const bool fits = pad16(D_.nx) <= maxRows && pad16(D_.nu) <= maxRows && pad16(D_.nxu) <= maxRows &&
+                          pad16(std::max(gNl(), gL())) <= maxRows && D_.nd <= 64 &&
+                          std::max({bLstar(), bLop(), bBack(), bFwd()}) <= 220 * 1024;
+        if (needsBatched() && !fits)
+            throw std::invalid_argument("[Cache] problem too large for the kernels that support its costs and constraints");
+        batched_ = fits && (B_ >= kTileB || needsBatched());
         if (!batched_) return;
         const HostProblem &p = hp_;
         const int nx = D_.nx, nu = D_.nu;
@@ -846,6 +982,14 @@ private:
         M_.K = padUpload(p.K, nu, nx, p.numNonleaf);
         M_.chol = padUpload(p.lowChol, nu, nu, p.numNonleaf);
         M_.AB = padUpload(p.AB, nx, nx + nu, p.numNodes);
+        if (gNl()) {
+            M_.nlG = padUpload(p.nlGamma, gNl(), D_.nxu, 1);
+            M_.nlGT = padUpload(p.nlGamma, D_.nxu, gNl(), 1, true);
+        }
+        if (gL()) {
+            M_.lG = padUpload(p.lGamma, gL(), nx, 1);
+            M_.lGT = padUpload(p.lGamma, nx, gL(), 1, true);
+        }
     }
 
     void allocate() {
@@ -877,6 +1021,8 @@ private:
         int *misc = dalloc<int>(4);
         S_.timeUp = misc; S_.active = misc + 1;
         devActive_ = misc + 2;
+        S_.tileLive = dalloc<int>((size_t)tiles);
+        allLive();
         CK(cudaMemset(misc, 0, 4 * sizeof(int)));
         CK(cudaMemset(ib, 0, Bi * 16 * sizeof(int)));
         CK(cudaMemset(db, 0, Bi * (8 + 2 * kMaxAnderson * kMaxAnderson) * sizeof(double)));
@@ -903,8 +1049,8 @@ private:
             optIn(k_lop_b<T, 0>, bLop(canDblLop()));
             optIn(k_lop_b<T, 1>, bLop(canDblLop()));
             optIn(k_lop_b<T, 2>, bLop(canDblLop()));
-            optIn(k_dyn_back_b<T>, bBack());
-            optIn(k_dyn_fwd_b<T>, bFwd());
+            optIn(k_dyn_back_b<T>, bBack(canDblBack()));
+            optIn(k_dyn_fwd_b<T>, bFwd(canDblFwd()));
             return;
         }
         optIn(k_dyn_back<T>, smBack());
@@ -924,6 +1070,18 @@ private:
 
     void fill(T *p, size_t n, T v) {
         k_fill<T><<<(int)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, stream_>>>(p, n, v);
+        CK(cudaGetLastError());
+    }
+
+    // Every tile live: before a solve's first round and before any launch outside a solve.
+    void allLive() {
+        const size_t tiles = (size_t)((B_ + 31) / 32);
+        k_fill<int><<<(int)((tiles + 255) / 256), 256, 0, stream_>>>(S_.tileLive, tiles, 1);
+        CK(cudaGetLastError());
+    }
+
+    void tileFlagsLaunch() {
+        k_tile_flags<<<(int)((B_ + 255) / 256), 256, 0, stream_>>>(S_.status, (int)B_, S_.tileLive);
         CK(cudaGetLastError());
     }
 
@@ -953,6 +1111,7 @@ private:
         OpArgs<T> A{};
         A.a1 = 1; A.a2 = 0; A.b1 = 1; A.b2 = 0; A.cL = 1;
         A.x0s = x0s_;
+        A.live = S_.tileLive;
         return A;
     }
 
@@ -981,19 +1140,22 @@ private:
 
     dim3 tileGrid(int nodes) const { return dim3((unsigned)((B_ + kTileB - 1) / kTileB), (unsigned)nodes); }
 
-    // L and L*: every node x groups of `tpc` instance tiles.
-    dim3 opGrid(int tpc) const {
+    // L and L*: every node x groups of `tpc` instance tiles; the dynamics sweep: every node of a stage.
+    dim3 opGridNodes(int tpc, int nodes) const {
         const long tiles = (B_ + kTileB - 1) / kTileB;
-        return dim3((unsigned)((tiles + tpc - 1) / tpc), (unsigned)D_.n);
+        return dim3((unsigned)((tiles + tpc - 1) / tpc), (unsigned)nodes);
     }
+    dim3 opGrid(int tpc) const { return opGridNodes(tpc, D_.n); }
 
-    // Autotuner of the L / L* tile shape: instance tiles per CTA in {1, 2, 4, 8}, double-buffered
-    // when more than one and the shared memory allows.  Each candidate is timed over 3 launches
-    // of the T-form kernel (CUDA events on the solver stream); the fastest is kept.  Runs once,
-    // before the round is captured; it writes only CAND and R, which every round rewrites first.
+    // Autotuner of the tile shapes of L, L* and the dynamics sweep: instance tiles per CTA in
+    // {1, 2, 4, 8}, double-buffered when more than one and the shared memory allows.  Each
+    // candidate is timed over 3 launches of the T-form kernel (or 3 whole sweeps), with CUDA events
+    // on the solver stream; the fastest is kept.  Runs once, before the round is captured; it
+    // writes only CAND, R and the sweep's workspaces, which every round rewrites first.
     void autotune() {
         if (!batched_ || tuned_) return;
         tuned_ = true;
+        allLive();
         const int tiles = (int)((B_ + kTileB - 1) / kTileB);
         cudaEvent_t e0, e1;
         CK(cudaEventCreate(&e0));
@@ -1023,6 +1185,18 @@ private:
         lstarDbl_ = tS > 1 && canDblLstar();
         tpcLop_ = tL;
         lopDbl_ = tL > 1 && canDblLop();
+        float bestD = 1e30f;
+        int tD = 1;
+        for (int tpc = 1; tpc <= kTilesPerCta && tpc <= tiles; tpc *= 2) {  // the whole sweep, both directions
+            tpcDyn_ = tpc;
+            backDbl_ = tpc > 1 && canDblBack();
+            fwdDbl_ = tpc > 1 && canDblFwd();
+            const float md = timeIt([&] { dynamics(); });
+            if (md < bestD) { bestD = md; tD = tpc; }
+        }
+        tpcDyn_ = tD;
+        backDbl_ = tD > 1 && canDblBack();
+        fwdDbl_ = tD > 1 && canDblFwd();
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
     }
@@ -1054,14 +1228,15 @@ private:
     void dynamics() {
         const int N = D_.ns - 1;
         if (batched_) {
+            const size_t smB = bBack(backDbl_), smF = bFwd(fwdDbl_);
             for (int st = N - 1; st >= 0; st--) {
-                k_dyn_back_b<T><<<tileGrid(stageCount_[st]), kTileB * kTileWarps, bBack(), stream_>>>(P_, D_, M_, CAND_, Q_, DD_,
-                                                                                                    stageFrom_[st], st);
+                k_dyn_back_b<T><<<opGridNodes(tpcDyn_, stageCount_[st]), kTileB * kTileWarps, smB, stream_>>>(
+                    P_, D_, M_, CAND_, Q_, DD_, stageFrom_[st], st, tpcDyn_, (int)backDbl_, S_.tileLive);
                 CK(cudaGetLastError());
             }
             for (int st = 0; st < N; st++) {
-                k_dyn_fwd_b<T><<<tileGrid(stageCount_[st]), kTileB * kTileWarps, bFwd(), stream_>>>(P_, D_, M_, CAND_, DD_, x0s_,
-                                                                                                   stageFrom_[st], Z_, R_);
+                k_dyn_fwd_b<T><<<opGridNodes(tpcDyn_, stageCount_[st]), kTileB * kTileWarps, smF, stream_>>>(
+                    P_, D_, M_, CAND_, DD_, x0s_, stageFrom_[st], Z_, R_, tpcDyn_, (int)fwdDbl_, S_.tileLive);
                 CK(cudaGetLastError());
             }
             return;
@@ -1125,6 +1300,14 @@ private:
         A.Z = Z_; A.CAND = CAND_; A.R = R_; A.PREV = PREV_; A.RPREV = RPREV_; A.BACKUP = BACKUP_; A.D = DIR_;
         A.ANDR = ANDR_; A.ANDZ = ANDZ_; A.action = S_.action; A.head = S_.head; A.useAnd = S_.useAnd;
         A.gamma = S_.gamma; A.tau = S_.tau; A.coef = S_.coef; A.m = (int)opt_.anderson;
+        if (B_ >= 32) {  // instance tiles x row chunks, about 8 blocks per SM
+            const long tiles = (B_ + 31) / 32;
+            const long chunks = std::max<long>(1, std::min<long>((152 * 8 + tiles - 1) / tiles, (D_.sZ + 7) / 8));
+            const long rows = (D_.sZ + chunks - 1) / chunks;
+            k_update_b<T><<<dim3((unsigned)tiles, (unsigned)((D_.sZ + rows - 1) / rows)), 256, 0, stream_>>>(D_, A, rows);
+            CK(cudaGetLastError());
+            return;
+        }
         const size_t total = (size_t)D_.sZ * B_;
         const int grid = (int)std::min<size_t>((total + 255) / 256, 152 * 8);
         k_update<T><<<grid, 256, 0, stream_>>>(D_, A);
@@ -1137,6 +1320,7 @@ private:
         reduceLaunch(kSpock, true);
         controlLaunch(kSpock);
         updateLaunch();
+        tileFlagsLaunch();
     }
 
     void ensureGraph() {

@@ -26,6 +26,7 @@ struct Dims {
     int n, nnl, nl, ns, nx, nu, nxu, ne, yD, nd;
     int costNl, costL, conNl, conL, affine;
     int dIII, dIV, dV, dVI;
+    int gNl, gL;  // rows of the nonleaf / leaf polyhedral constraint matrices Gamma
     long oX, oY, oT, oS, sPrim;              // primal offsets
     long oI, oII, oIII, oIV, oV, oVI, sDual;  // dual offsets, absolute (dual starts at sPrim)
     long sZ;
@@ -41,6 +42,7 @@ struct DevProblem {
     const T *lSqrtQ, *lq, *lTrans;
     const T *nlLo, *nlHi, *lLo, *lHi;
     const T *NNtr, *b;
+    const T *grad, *lGrad;  // linear costs: gradient per node ((nx + nu) x n) and of the leaves (nx)
     T step;
 };
 
@@ -56,6 +58,7 @@ struct OpArgs {
     T *outBase;     // when set, base is stored here too
     T *outR;        // mode 0: the residual Z - out of every entry finalized by this kernel
     const T *x0s;   // scaled initial states, nx x B
+    const int *live;  // per tile of 32 instances: nonzero while one of them runs (null: all)
 };
 
 struct Options {
@@ -71,6 +74,7 @@ struct DevState {
     int *k0, *k1, *k2, *k2bt, *k3, *calls;
     double *tau, *zeta, *w, *wSafe, *tol, *err, *coef, *G, *gamma;
     int *timeUp, *active;
+    int *tileLive;  // per tile of 32 instances: nonzero while one of them is running
 };
 
 class EngineBase {
@@ -86,18 +90,24 @@ public:
     virtual void getFirstInputs(double *out) = 0;  // unscaled u_0, B*nu
     virtual void getStatus(int *status, long *iters) = 0;
     virtual void getCounters(long *out7) = 0;  // instance 0: k0,k1,k2,k2bt,k3,calls,iters
+    virtual void getCountersAll(long *out) = 0;  // every instance: B x 7, same order
     virtual void op(const double *prim, double *dual) = 0;
     virtual void adj(const double *dual, double *prim) = 0;
     virtual void cpStep(const double *x0, const double *z, double *cand) = 0;
     virtual void applyM(const double *z, double *mz) = 0;
     virtual int precisionBits() const = 0;
+    // The current iterate on the device (sZ x batch, element-major, in the solver precision), and
+    // its replacement by another solver's iterate of the same problem size and batch, converted
+    // to this solver's precision on the device (an FP32 solve handing over to an FP64 polish).
+    virtual const void *iterateDevice() const = 0;
+    virtual void setIterateFromDevice(const void *src, int srcBits, long sZ, long batch, int srcDevice) = 0;
     virtual double lastSeconds() const = 0;
     virtual double kernelMs(const char *which, int reps) = 0;  // CUDA-event timing of one kernel
     virtual void timedRounds(int rounds, float *ms) = 0;
     virtual long bytesPerRoundAlgorithmic(const char *which) const = 0;
     virtual int launchesPerRound() const = 0;
-    // Tile shapes in use: L* instance tiles per CTA, L* double-buffered, the same for L,
-    // batched kernels (1) or the small-batch ones (0).  Runs the autotuner if it has not run.
+    // Tile shapes in use: L* instance tiles per CTA, L* double-buffered, the same for L, and the
+    // dynamics sweep's tiles per CTA (0: the small-batch kernels).  Runs the autotuner if needed.
     virtual void tuning(int *out5) = 0;
     long lastRounds() const { return lastRounds_; }
     int device() const { return device_; }

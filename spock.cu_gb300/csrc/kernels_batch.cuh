@@ -41,6 +41,7 @@ struct PadMats {
     const T *BTr, *APB, *ABKTr;      // per node (child j)
     const T *Kt, *K, *chol;          // per nonleaf node: K' (nx x nu), K (nu x nx), lower Cholesky (nu x nu)
     const T *AB;                     // per node: [A B] (nx x nxu)
+    const T *nlG, *nlGT, *lG, *lGT;  // polyhedral constraints: Gamma and Gamma' (nonleaf, leaf)
 };
 
 __device__ __forceinline__ unsigned smemAddr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -174,18 +175,35 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem
     const bool nonleaf = i < D.nnl;
     const int c0 = nonleaf ? P.chFrom[i] : 0, nc = nonleaf ? P.numCh[i] : 0;
     const int l = i - D.nnl;
-    const bool rect = nonleaf ? D.conNl == kConRectangle : D.conL == kConRectangle;
+    // constraint rows: identity part (rectangle, polyhedron with identity) and Gamma part
+    // (polyhedron, polyhedron with identity); linear costs have 2-row IV / VI blocks [g'xu | t]
+    const int con = nonleaf ? D.conNl : D.conL;
+    const int nId = (con == kConRectangle || con == kConPolyhedronWithIdentity) ? (nonleaf ? nxu : nx) : 0;
+    const int nG = (con == kConPolyhedron || con == kConPolyhedronWithIdentity) ? (nonleaf ? D.gNl : D.gL) : 0;
+    const bool linNl = D.costNl == kCostLinear, linL = D.costL == kCostLinear;
     // input row map
-    const int rIII = nc * dIV, rI = rIII + (rect ? nxu : 0), rII = rI + yD, rS = rII + 1;
-    const int nIn = nonleaf ? rS + 2 * nc : dVI + (rect ? nx : 0);
+    const int rIII = nc * dIV, rIIIg = rIII + (nonleaf ? nId : 0), rI = rIIIg + (nonleaf ? nG : 0);
+    const int rII = rI + yD, rS = rII + 1, rRootT = rS + 2 * nc;
+    const int nIn = nonleaf ? rRootT + (linNl && i == 0 ? 1 : 0) : dVI + nId + nG;
+    auto rowIV = [&](int j, int q) -> long {  // row q of IV_j
+        if (linNl) return q == 0 ? D.oIV + j : D.oIV + D.n + j;
+        return D.oIV + (long)j * dIV + q;
+    };
     auto rowIn = [&](int r) -> long {
-        if (!nonleaf) return r < dVI ? D.oVI + (long)l * dVI + r : D.oV + (long)l * nx + (r - dVI);
-        if (r < rIII) return D.oIV + (long)(c0 + r / dIV) * dIV + r % dIV;
-        if (r < rI) return D.oIII + (long)i * nxu + (r - rIII);
+        if (!nonleaf) {
+            if (r < dVI) return linL ? (r == 0 ? D.oVI + l : D.oVI + D.nl + l) : D.oVI + (long)l * dVI + r;
+            if (r < dVI + nId) return D.oV + (long)l * nx + (r - dVI);
+            return D.oV + (con == kConPolyhedron ? 0 : (long)D.nl * nx) + (long)l * D.gL + (r - dVI - nId);
+        }
+        if (r < rIII) return rowIV(c0 + r / dIV, r % dIV);
+        if (r < rIIIg) return D.oIII + (long)i * nxu + (r - rIII);
+        if (r < rI) return D.oIII + (con == kConPolyhedron ? 0 : (long)D.nnl * nxu) + (long)i * D.gNl + (r - rIIIg);
         if (r < rII) return D.oI + (long)i * yD + (r - rI);
         if (r == rII) return D.oII + i;
+        if (r == rRootT) return D.oIV + D.n;  // t_0 of a linear cost
         const int jj = (r - rS) >> 1, j = c0 + jj;
         if (j < D.nnl) return D.oII + j;
+        if (linL) return D.oVI + D.nl + (j - D.nnl);  // both rows: s_l itself, 0.5 (s + s) = s
         return D.oVI + (long)(j - D.nnl) * dVI + nx + ((r - rS) & 1);
     };
     const int bY = nxu, bT = bY + yD, bS = bT + nc, bRoot = bS + nc;
@@ -200,12 +218,16 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem
     };
     const int inArr = A.in2 ? 2 : 1, baseArr = A.base2 ? 2 : (A.base1 ? 1 : 0);
     const int ldx = pad16(nx), ldu = pad16(nu);
-    const int perChild = ldx * nx + ldu * nu + ldx + ldu;
-    const int matElems = nonleaf ? nc * perChild : ldx * nx + ldx;
+    const int perChild = linNl ? 0 : ldx * nx + ldu * nu + ldx + ldu;
+    const int dG = nonleaf ? nxu : nx;  // Gamma' has dG rows (padded) and nG columns
+    const int matG = nG ? pad16(dG) * nG : 0;
+    const int matElems = (nonleaf ? nc * perChild : (linL ? 0 : ldx * nx + ldx)) + matG;
     const int bufElems = (nIn * inArr + nBase * baseArr) * kTileB;  // one tile's input and base rows
-    T *sMat = sm, *sBuf = sMat + matElems;
+    T *sMat = sm, *sGT = sMat + matElems - matG, *sBuf = sMat + matElems;
     T *sAv = sBuf + (dbl ? 2 : 1) * bufElems;  // the 4E+1 vector of the kernel projection
-    if (nonleaf) {
+    T *sGv = sAv + D.nd * kTileB;              // Gamma' times the constraint rows, dG x 32
+    if (nG) stageMat(sGT, nonleaf ? M.nlGT : M.lGT, matG);
+    if (nonleaf && !linNl) {
         const bool qplNl = D.costNl == kCostQuadraticPlusLinear;
         for (int jj = 0; jj < nc; jj++) {
             const int j = c0 + jj;
@@ -217,7 +239,7 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem
                 stageMat(m + ldx * nx + ldu * nu + ldx, M.r + (size_t)j * ldu, ldu);
             }
         }
-    } else {
+    } else if (!nonleaf && !linL) {
         stageMat(sMat, M.lSqrtQ, ldx * nx);
         if (D.costL == kCostQuadraticPlusLinear) stageMat(sMat + ldx * nx, M.lq, ldx);
     }
@@ -225,14 +247,29 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem
     // flight while tile t is computed; the node's matrices are staged once for all of them.
     const int nTiles = (B + kTileB - 1) / kTileB;
     const int t0 = blockIdx.x * tilesPerCta, t1 = min(t0 + tilesPerCta, nTiles);
+    auto live = [&](int t) { return !A.live || A.live[t] != 0; };
+    {  // nothing to do when every instance of this CTA's tiles has stopped
+        bool any = false;
+        for (int t = t0; t < t1; t++) any = any || live(t);
+        if (!any) return;
+    }
+    // The node's row maps, evaluated once per CTA into shared memory: every tile's gathers and
+    // output writes then take their iterate rows from these tables.
+    int *sRowIn = reinterpret_cast<int *>(sGv + (nG ? dG : 0) * kTileB), *sRowBase = sRowIn + nIn;
+    for (int r = threadIdx.x; r < nIn; r += blockDim.x) sRowIn[r] = (int)rowIn(r);
+    for (int r = threadIdx.x; r < nBase; r += blockDim.x) sRowBase[r] = (int)rowBase(r);
+    __syncthreads();
+    auto tabIn = [&](int r) -> long { return sRowIn[r]; };
+    auto tabBase = [&](int r) -> long { return sRowBase[r]; };
     auto prefetch = [&](int t) {
+        if (!live(t)) return;
         T *buf = sBuf + (dbl ? ((t - t0) & 1) * bufElems : 0);
         const int bb = t * kTileB;
-        gather(buf, nIn, A.in1, B, bb, lane, warp, rowIn);
-        if (A.in2) gather(buf + nIn * kTileB, nIn, A.in2, B, bb, lane, warp, rowIn);
+        gather(buf, nIn, A.in1, B, bb, lane, warp, tabIn);
+        if (A.in2) gather(buf + nIn * kTileB, nIn, A.in2, B, bb, lane, warp, tabIn);
         T *bs = buf + nIn * inArr * kTileB;
-        if (A.base1) gather(bs, nBase, A.base1, B, bb, lane, warp, rowBase);
-        if (A.base2) gather(bs + nBase * kTileB, nBase, A.base2, B, bb, lane, warp, rowBase);
+        if (A.base1) gather(bs, nBase, A.base1, B, bb, lane, warp, tabBase);
+        if (A.base2) gather(bs + nBase * kTileB, nBase, A.base2, B, bb, lane, warp, tabBase);
     };
     if (t0 < t1) prefetch(t0);
     cpAsyncCommit();
@@ -244,6 +281,7 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem
         const T *sIn = sBuf + (dbl ? ((tile - t0) & 1) * bufElems : 0), *sBase = sIn + nIn * inArr * kTileB;
         const int b0 = tile * kTileB, b = b0 + lane;
         const bool act = b < B;
+        auto tileBody = [&]() {
         auto IN = [&](int r) -> T {
             T v = A.a1 * sIn[r * kTileB + lane];
             if (inArr == 2) v += A.a2 * sIn[(nIn + r) * kTileB + lane];
@@ -258,15 +296,35 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem
         auto EMIT = [&](int rb, T lv) {
             if (!act) return;
             const T bs = BASE(rb);
-            const size_t o = (size_t)rowBase(rb) * B + b;
+            const size_t o = (size_t)sRowBase[rb] * B + b;
             if (A.outBase) A.outBase[o] = bs;
             A.out[o] = bs + A.cL * lv;
         };
         auto FIN = [&](int rb, T val) {  // a final primal entry (mode 0) and its residual
             if (!act) return;
-            const size_t o = (size_t)rowBase(rb) * B + b;
+            const size_t o = (size_t)sRowBase[rb] * B + b;
             A.out[o] = val;
             if (A.outR) A.outR[o] = BASE(rb) - val;
+        };
+        if (nG) {  // Gamma' times the Gamma rows of III (or V) into shared memory (constraints.cuh:272-285, 410-425)
+            T accG[kMaxTasks][kRT];
+            zeroAcc(accG);
+            const int rg = nonleaf ? rIIIg : dVI + nId;
+            gemv(accG, sGT, dG, nG, warp, [&](int k) { return IN(rg + k); });
+    #pragma unroll
+            for (int q = 0; q < kMaxTasks; q++) {
+                const int r0 = (warp + q * kTileWarps) * kRT;
+    #pragma unroll
+                for (int t = 0; t < kRT; t++)
+                    if (r0 + t < dG) sGv[(r0 + t) * kTileB + lane] = accG[q][t];
+            }
+            __syncthreads();
+        }
+        // constraint part of x_i / u_i (row r of [x; u]): identity rows and Gamma' rows
+        auto conPart = [&](int r, int rId) -> T {
+            T v = nId ? IN(rId + r) : T(0);
+            if (nG) v += sGv[r * kTileB + lane];
+            return v;
         };
         T accX[kMaxTasks][kRT], accU[kMaxTasks][kRT];
         zeroAcc(accX);
@@ -274,7 +332,13 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem
         if (nonleaf) {
             const bool qpl = D.costNl == kCostQuadraticPlusLinear;
             const int sx = warp, su = slotFrom(warp, tasksOf(nx));  // x and u blocks on different warps
-            for (int jj = 0; jj < nc; jj++) {
+            auto linPart = [&](int r) -> T {  // linear costs: sum over children of g_j[r] * IV_j
+                T v = 0;
+                if (linNl)
+                    for (int jj = 0; jj < nc; jj++) v += __ldg(P.grad + (size_t)(c0 + jj) * nxu + r) * IN(jj * dIV);
+                return v;
+            };
+            for (int jj = 0; jj < nc && !linNl; jj++) {
                 const int r0 = jj * dIV;
                 const T *m = sMat + jj * perChild;
                 gemv(accX, m, nx, nx, sx, [&](int k) { return IN(r0 + k); });
@@ -290,8 +354,8 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem
                 const int rx0 = (sx + q * kTileWarps) * kRT, ru0 = (su + q * kTileWarps) * kRT;
     #pragma unroll
                 for (int t = 0; t < kRT; t++) {
-                    if (rx0 + t < nx) EMIT(rx0 + t, accX[q][t] + (rect ? IN(rIII + rx0 + t) : T(0)));
-                    if (ru0 + t < nu) EMIT(nx + ru0 + t, accU[q][t] + (rect ? IN(rIII + nx + ru0 + t) : T(0)));
+                    if (rx0 + t < nx) EMIT(rx0 + t, accX[q][t] + conPart(rx0 + t, rIII) + linPart(rx0 + t));
+                    if (ru0 + t < nu) EMIT(nx + ru0 + t, accU[q][t] + conPart(nx + ru0 + t, rIII) + linPart(nx + ru0 + t));
                 }
             }
             // y_i, the children's t and s, and the AVaR kernel projection (cache.cuh:650-676): entry
@@ -305,9 +369,9 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem
             };
             auto avarLin = [&](int k) -> T {  // the L* part of entry k
                 if (k < yD) return IN(rI + k) - P.b[(size_t)i * yD + k] * II;
-                if (k < yD + D.ne) {
+                if (k < yD + D.ne) {  // t_j: half the sum of the last two IV rows, or IV's t row (linear)
                     const int jj = k - yD;
-                    return T(0.5) * (IN(jj * dIV + nxu) + IN(jj * dIV + nxu + 1));
+                    return linNl ? IN(jj * dIV + 1) : T(0.5) * (IN(jj * dIV + nxu) + IN(jj * dIV + nxu + 1));
                 }
                 const int jj = k - yD - D.ne;
                 return (c0 + jj < D.nnl) ? IN(rS + 2 * jj) : T(0.5) * (IN(rS + 2 * jj) + IN(rS + 2 * jj + 1));
@@ -333,21 +397,24 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem
                 }
             }
             if (warp == 0) {
-                if (i == 0) {  // t_0 carries no cost term; s_0 gets the prox of the objective
+                if (i == 0) {  // t_0: no cost term (or IV's t row of a linear cost); s_0 gets the prox of the objective
+                    const T t0 = linNl ? IN(rRootT) : T(0);
                     if (MODE == 0) {
-                        FIN(bRoot, BASE(bRoot));
+                        FIN(bRoot, BASE(bRoot) + A.cL * t0);
                         FIN(bRoot + 1, BASE(bRoot + 1) + A.cL * II - P.step);
                     } else {
-                        EMIT(bRoot, T(0));
+                        EMIT(bRoot, t0);
                         EMIT(bRoot + 1, II);
                     }
                 }
             }
         } else {
-            gemv(accX, sMat, nx, nx, warp, [&](int k) { return IN(k); });
-            if (D.costL == kCostQuadraticPlusLinear) {
-                const T d23 = T(-0.5) * (IN(nx) + IN(nx + 1));
-                gemv(accX, sMat + ldx * nx, nx, 1, warp, [&](int) { return d23; });
+            if (!linL) {
+                gemv(accX, sMat, nx, nx, warp, [&](int k) { return IN(k); });
+                if (D.costL == kCostQuadraticPlusLinear) {
+                    const T d23 = T(-0.5) * (IN(nx) + IN(nx + 1));
+                    gemv(accX, sMat + ldx * nx, nx, 1, warp, [&](int) { return d23; });
+                }
             }
     #pragma unroll
             for (int q = 0; q < kMaxTasks; q++) {
@@ -355,10 +422,12 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem
     #pragma unroll
                 for (int t = 0; t < kRT; t++) {
                     const int r = r0 + t;
-                    if (r < nx) EMIT(r, accX[q][t] + (rect ? IN(dVI + r) : T(0)));
+                    if (r < nx) EMIT(r, accX[q][t] + conPart(r, dVI) + (linL ? __ldg(P.lGrad + r) * IN(0) : T(0)));
                 }
             }
         }
+        };
+        if (live(tile)) tileBody();
         __syncthreads();  // every warp is done with this tile's rows before the buffer is refilled
         if (!dbl && tile + 1 < t1) prefetch(tile + 1);
     }
@@ -381,7 +450,12 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T
     const bool nonleaf = j < D.nnl;
     const int l = j - D.nnl;
     const int a = j > 0 ? P.anc[j] : 0;
-    const bool rect = nonleaf ? D.conNl == kConRectangle : D.conL == kConRectangle;
+    // constraint rows of this node: an identity part (rectangle, polyhedron with identity) and a
+    // Gamma part (polyhedron, polyhedron with identity); linear costs have a 2-row IV / VI
+    const int con = nonleaf ? D.conNl : D.conL;
+    const int nId = (con == kConRectangle || con == kConPolyhedronWithIdentity) ? (nonleaf ? nxu : nx) : 0;
+    const int nG = (con == kConPolyhedron || con == kConPolyhedronWithIdentity) ? (nonleaf ? D.gNl : D.gL) : 0;
+    const bool linNl = D.costNl == kCostLinear, linL = D.costL == kCostLinear;
     const T g = P.step, gi = T(1) / P.step;
     const int rOwn = nxu + 1;
     const int nIn = nonleaf ? rOwn + yD + 1 + nxu : rOwn + nx + 1;
@@ -399,42 +473,69 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T
         if (q < nx) return D.oX + (long)j * nx + q;
         return D.oS + j;
     };
-    const int bIII = yD + 1, bIVn = bIII + (rect ? nxu : 0);
-    const int bIV = nonleaf ? bIVn : 0, bV = dIV, bVI = dIV + (rect ? nx : 0);
+    const int bIII = yD + 1, bIIIg = bIII + nId, bIVn = bIIIg + nG;
+    const int bIV = nonleaf ? bIVn : 0, bV = dIV, bVg = bV + nId, bVI = bVg + nG;
     const int nBase = nonleaf ? bIVn + dIV : bVI + dVI;
+    auto rowIV = [&](int q) -> long {  // row q of IV_j: per node (quadratic), or [g'xu | t] (linear)
+        if (linNl) return q == 0 ? D.oIV + j : D.oIV + D.n + j;
+        return D.oIV + (long)j * dIV + q;
+    };
     auto rowBase = [&](int r) -> long {
         if (nonleaf) {
             if (r < yD) return D.oI + (long)j * yD + r;
             if (r == yD) return D.oII + j;
-            if (r < bIVn) return D.oIII + (long)j * nxu + (r - bIII);
-            return D.oIV + (long)j * dIV + (r - bIVn);
+            if (r < bIIIg) return D.oIII + (long)j * nxu + (r - bIII);
+            if (r < bIVn)
+                return D.oIII + (con == kConPolyhedron ? 0 : (long)D.nnl * nxu) + (long)j * D.gNl + (r - bIIIg);
+            return rowIV(r - bIVn);
         }
-        if (r < bV) return D.oIV + (long)j * dIV + r;
-        if (r < bVI) return D.oV + (long)l * nx + (r - bV);
+        if (r < bV) return rowIV(r);
+        if (r < bVg) return D.oV + (long)l * nx + (r - bV);
+        if (r < bVI) return D.oV + (con == kConPolyhedron ? 0 : (long)D.nl * nx) + (long)l * D.gL + (r - bVg);
+        if (linL) return r == bVI ? D.oVI + l : D.oVI + D.nl + l;
         return D.oVI + (long)l * dVI + (r - bVI);
     };
     const int inArr = A.in2 ? 2 : 1, baseArr = A.base2 ? 2 : (A.base1 ? 1 : 0);
     const int dSoc = dIV > dVI ? dIV : dVI;
     const int ldx = pad16(nx), ldu = pad16(nu);
-    const int matIV = ldx * nx + ldu * nu, matElems = matIV + (nonleaf ? 0 : ldx * nx);
+    const int matIV = linNl ? 0 : ldx * nx + ldu * nu, matVI = (!nonleaf && !linL) ? ldx * nx : 0;
+    const int matG = nG ? pad16(nG) * (nonleaf ? nxu : nx) : 0;  // Gamma, padded column-major
+    const int matElems = matIV + matVI + matG;
     const int bufElems = (nIn * inArr + nBase * baseArr) * kTileB;  // one tile's input and base rows
     T *sMat = sm, *sw = sMat + matElems, *sPart = sw + dSoc * kTileB, *sBuf = sPart + kTileWarps * kTileB;
-    if (j > 0) {
+    T *sG = sMat + matIV + matVI;
+    if (j > 0 && !linNl) {
         stageMat(sMat, M.sqrtQ + (size_t)j * ldx * nx, ldx * nx);
         stageMat(sMat + ldx * nx, M.sqrtR + (size_t)j * ldu * nu, ldu * nu);
     }
-    if (!nonleaf) stageMat(sMat + matIV, M.lSqrtQ, ldx * nx);
+    if (matVI) stageMat(sMat + matIV, M.lSqrtQ, ldx * nx);
+    if (nG) stageMat(sG, nonleaf ? M.nlG : M.lG, matG);
     // This CTA's instance tiles [t0, t1), double-buffered as in k_lstar_b.
     const int nTiles = (B + kTileB - 1) / kTileB;
     const int t0 = blockIdx.x * tilesPerCta, t1 = min(t0 + tilesPerCta, nTiles);
+    auto live = [&](int t) { return !A.live || A.live[t] != 0; };
+    {  // nothing to do when every instance of this CTA's tiles has stopped
+        bool any = false;
+        for (int t = t0; t < t1; t++) any = any || live(t);
+        if (!any) return;
+    }
+    // The node's row maps, evaluated once per CTA into shared memory: every tile's gathers and
+    // output writes then take their iterate rows from these tables.
+    int *sRowIn = reinterpret_cast<int *>(sBuf + (dbl ? 2 : 1) * bufElems), *sRowBase = sRowIn + nIn;
+    for (int r = threadIdx.x; r < nIn; r += blockDim.x) sRowIn[r] = (int)rowIn(r);
+    for (int r = threadIdx.x; r < nBase; r += blockDim.x) sRowBase[r] = (int)rowBase(r);
+    __syncthreads();
+    auto tabIn = [&](int r) -> long { return sRowIn[r]; };
+    auto tabBase = [&](int r) -> long { return sRowBase[r]; };
     auto prefetch = [&](int t) {
+        if (!live(t)) return;
         T *buf = sBuf + (dbl ? ((t - t0) & 1) * bufElems : 0);
         const int bb = t * kTileB;
-        gather(buf, nIn, A.in1, B, bb, lane, warp, rowIn);
-        if (A.in2) gather(buf + nIn * kTileB, nIn, A.in2, B, bb, lane, warp, rowIn);
+        gather(buf, nIn, A.in1, B, bb, lane, warp, tabIn);
+        if (A.in2) gather(buf + nIn * kTileB, nIn, A.in2, B, bb, lane, warp, tabIn);
         T *bs = buf + nIn * inArr * kTileB;
-        if (A.base1) gather(bs, nBase, A.base1, B, bb, lane, warp, rowBase);
-        if (A.base2) gather(bs + nBase * kTileB, nBase, A.base2, B, bb, lane, warp, rowBase);
+        if (A.base1) gather(bs, nBase, A.base1, B, bb, lane, warp, tabBase);
+        if (A.base2) gather(bs + nBase * kTileB, nBase, A.base2, B, bb, lane, warp, tabBase);
     };
     if (t0 < t1) prefetch(t0);
     cpAsyncCommit();
@@ -446,6 +547,7 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T
         const T *sIn = sBuf + (dbl ? ((tile - t0) & 1) * bufElems : 0), *sBase = sIn + nIn * inArr * kTileB;
         const int b0 = tile * kTileB, b = b0 + lane;
         const bool act = b < B;
+        auto tileBody = [&]() {
         auto INP = [&](int r) -> T {
             T v = A.a1 * sIn[r * kTileB + lane];
             if (inArr == 2) v += A.a2 * sIn[(nIn + r) * kTileB + lane];
@@ -460,13 +562,13 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T
         auto EMIT = [&](int rb, T lv) {
             if (!act) return;
             const T bs = BASE(rb);
-            const size_t o = (size_t)rowBase(rb) * B + b;
+            const size_t o = (size_t)sRowBase[rb] * B + b;
             if (A.outBase) A.outBase[o] = bs;
             A.out[o] = bs + A.cL * lv;
         };
         auto FIN = [&](int rb, T val) {  // a final dual entry (mode 0) and its residual
             if (!act) return;
-            const size_t o = (size_t)rowBase(rb) * B + b;
+            const size_t o = (size_t)sRowBase[rb] * B + b;
             A.out[o] = val;
             if (A.outR) A.outR[o] = BASE(rb) - val;
         };
@@ -508,17 +610,45 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T
                     FIN(yD, (v - (v > T(0) ? v : T(0))) * g);
                 } else EMIT(yD, lv);
             }
-            if (rect)
-                for (int k = warp; k < nxu; k += kTileWarps) {
-                    const T lv = k < nx ? INP(rx + k) : INP(ru + k - nx);
-                    if (MODE == 0) {
-                        const T v = (BASE(bIII + k) + A.cL * lv) * gi;
-                        const T pr = boxProject(v, P.nlLo[(size_t)j * nxu + k], P.nlHi[(size_t)j * nxu + k]);
-                        FIN(bIII + k, (v - pr) * g);
-                    } else EMIT(bIII + k, lv);
+            auto boxRow = [&](int rb, T lv) {  // III row: [x; u] or Gamma [x; u], box bounds (constraints.cuh:70-74)
+                if (MODE == 0) {
+                    const size_t bi = (size_t)(sRowBase[rb] - D.oIII);
+                    const T v = (BASE(rb) + A.cL * lv) * gi;
+                    FIN(rb, (v - boxProject(v, P.nlLo[bi], P.nlHi[bi])) * g);
+                } else EMIT(rb, lv);
+            };
+            for (int k = warp; k < nId; k += kTileWarps) boxRow(bIII + k, k < nx ? INP(rx + k) : INP(ru + k - nx));
+            if (nG) {  // Gamma [x_j; u_j] (constraints.cuh:251-264, 386-401)
+                T accG[kMaxTasks][kRT];
+                zeroAcc(accG);
+                gemv(accG, sG, nG, nxu, warp, [&](int k) { return INP(rx + k); });
+    #pragma unroll
+                for (int q = 0; q < kMaxTasks; q++) {
+                    const int r0 = (warp + q * kTileWarps) * kRT;
+    #pragma unroll
+                    for (int t = 0; t < kRT; t++)
+                        if (r0 + t < nG) boxRow(bIIIg + r0 + t, accG[q][t]);
                 }
+            }
         }
-        {  // IV_j = [sqrtQ_j x_a; sqrtR_j u_a; h; h] (costs.cuh:126-161, 379-417); zero at the root
+        auto linEpi = [&](int rb, T lv0, T lv1) {  // linear-cost epigraph rows (costs.cuh:261-301)
+            if (MODE == 0) {
+                const T v0 = (BASE(rb) + A.cL * lv0) * gi, v1 = (BASE(rb + 1) + A.cL * lv1) * gi;
+                FIN(rb, (v0 - (v0 < v1 ? v0 : v1)) * g);  // the first entry is clamped from above by the second
+                FIN(rb + 1, T(0));
+            } else {
+                EMIT(rb, lv0);
+                EMIT(rb + 1, lv1);
+            }
+        };
+        if (linNl) {  // IV_j = [g_j'(x_a, u_a); t_j]; the root has no g term
+            if (warp == 0) {
+                T lin = 0;
+                if (j > 0)
+                    for (int k = 0; k < nxu; k++) lin += __ldg(P.grad + (size_t)j * nxu + k) * INP(k);
+                linEpi(bIV, lin, INP(nxu));
+            }
+        } else {  // IV_j = [sqrtQ_j x_a; sqrtR_j u_a; h; h] (costs.cuh:126-161, 379-417); zero at the root
             T accX[kMaxTasks][kRT], accU[kMaxTasks][kRT];
             zeroAcc(accX);
             zeroAcc(accU);
@@ -568,15 +698,34 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T
         }
         if (!nonleaf) {  // V and VI of a leaf (constraints.cuh:168-170, costs.cuh:149-161/404-417)
             const int rx = rOwn, rs = rOwn + nx;
-            if (rect)
-                for (int k = warp; k < nx; k += kTileWarps) {
-                    const T lv = INP(rx + k);
-                    if (MODE == 0) {
-                        const T v = (BASE(bV + k) + A.cL * lv) * gi;
-                        const T pr = boxProject(v, P.lLo[(size_t)l * nx + k], P.lHi[(size_t)l * nx + k]);
-                        FIN(bV + k, (v - pr) * g);
-                    } else EMIT(bV + k, lv);
+            auto boxRowL = [&](int rb, T lv) {
+                if (MODE == 0) {
+                    const size_t bi = (size_t)(sRowBase[rb] - D.oV);
+                    const T v = (BASE(rb) + A.cL * lv) * gi;
+                    FIN(rb, (v - boxProject(v, P.lLo[bi], P.lHi[bi])) * g);
+                } else EMIT(rb, lv);
+            };
+            for (int k = warp; k < nId; k += kTileWarps) boxRowL(bV + k, INP(rx + k));
+            if (nG) {
+                T accG[kMaxTasks][kRT];
+                zeroAcc(accG);
+                gemv(accG, sG, nG, nx, warp, [&](int k) { return INP(rx + k); });
+    #pragma unroll
+                for (int q = 0; q < kMaxTasks; q++) {
+                    const int r0 = (warp + q * kTileWarps) * kRT;
+    #pragma unroll
+                    for (int t = 0; t < kRT; t++)
+                        if (r0 + t < nG) boxRowL(bVg + r0 + t, accG[q][t]);
                 }
+            }
+            if (linL) {  // VI_l = [g'x_l; s_l]
+                if (warp == 0) {
+                    T lin = 0;
+                    for (int k = 0; k < nx; k++) lin += __ldg(P.lGrad + k) * INP(rx + k);
+                    linEpi(bVI, lin, INP(rs));
+                }
+                return;  // nothing else in this tile; the caller's barrier follows
+            }
             T accX[kMaxTasks][kRT];
             zeroAcc(accX);
             gemv(accX, sMat + matIV, nx, nx, warp, [&](int k) { return INP(rx + k); });
@@ -615,6 +764,8 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T
                     for (int r = nx; r < dVI; r++) EMIT(bVI + r, h);
             }
         }
+        };
+        if (live(tile)) tileBody();
         __syncthreads();  // every warp is done with this tile's rows (and sw) before they are refilled
         if (!dbl && tile + 1 < t1) prefetch(tile + 1);
     }
@@ -622,25 +773,26 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T
 
 // ------------------------------------------------------------------------------------------
 // Dynamics projection, one stage of the backward sweep (dynamics.cuh:85-139).
-// inputs: q of the children (-x of leaves at the last stage, else Q), u_i, x_i
+// inputs per instance tile: q of the children (-x of leaves at the last stage, else Q), u_i, x_i.
+// A CTA stages node i's matrices once and runs `tilesPerCta` instance tiles, double-buffered
+// when `dbl` (the rows of tile t + 1 load while tile t is computed).
 // ------------------------------------------------------------------------------------------
 template <typename T>
 __global__ void __launch_bounds__(kTileB *kTileWarps) k_dyn_back_b(const DevProblem<T> P, const Dims D, const PadMats<T> M,
                                                                   const T *__restrict__ cand, T *__restrict__ Q,
-                                                                  T *__restrict__ DD, int stageFrom, int stage) {
+                                                                  T *__restrict__ DD, int stageFrom, int stage,
+                                                                  int tilesPerCta, int dbl, const int *live) {
     extern __shared__ __align__(16) unsigned char smraw[];
     T *sm = reinterpret_cast<T *>(smraw);
     const int B = D.B, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int b0 = blockIdx.x * kTileB, b = b0 + lane;
-    const bool act = b < B;
     const int i = stageFrom + blockIdx.y;
     const int nx = D.nx, nu = D.nu;
     const int c0 = P.chFrom[i], nc = P.numCh[i];
     const bool leafChildren = c0 >= D.nnl;
     const int ldx = pad16(nx), ldu = pad16(nu);
     const int perChild = ldu * nx + ldx * nu + ldx * nx;  // B', APB, (A+BK)'
-    T *sMat = sm, *sKt = sMat + nc * perChild, *sL = sKt + ldx * nu;
-    T *sq = sL + ldu * nu, *su = sq + nc * nx * kTileB, *sx = su + nu * kTileB, *sd = sx + nx * kTileB;
+    const int bufElems = (nc * nx + nu + nx) * kTileB;   // one tile's q, u and x rows
+    T *sMat = sm, *sKt = sMat + nc * perChild, *sL = sKt + ldx * nu, *sd = sL + ldu * nu, *sBuf = sd + nu * kTileB;
     for (int jj = 0; jj < nc; jj++) {
         const int j = c0 + jj;
         T *m = sMat + jj * perChild;
@@ -652,158 +804,211 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_dyn_back_b(const DevProb
     }
     if (stage > 0) stageMat(sKt, M.Kt + (size_t)i * ldx * nu, ldx * nu);
     stageMat(sL, M.chol + (size_t)i * ldu * nu, ldu * nu);
-    if (leafChildren)
-        gather(sq, nc * nx, cand, B, b0, lane, warp, [&](int r) { return D.oX + (long)c0 * nx + r; });
-    else
-        gather(sq, nc * nx, (const T *)Q, B, b0, lane, warp, [&](int r) { return (long)c0 * nx + r; });
-    gather(su, nu, cand, B, b0, lane, warp, [&](int r) { return (long)i * nu + r; });
-    if (stage > 0) gather(sx, nx, cand, B, b0, lane, warp, [&](int r) { return D.oX + (long)i * nx + r; });
-    cpAsyncWaitAll();
-    __syncthreads();
-    if (leafChildren || D.affine) {  // q of a leaf is -x; affine dynamics add P e (dynamics.cuh:96-99)
-        for (int t = warp; t < nc * nx; t += kTileWarps) {
-            T v = sq[t * kTileB + lane];
-            if (leafChildren) v = -v;
-            if (D.affine) v += P.Pe[(size_t)c0 * nx + t];
-            sq[t * kTileB + lane] = v;
+    const int nTiles = (B + kTileB - 1) / kTileB;
+    const int t0 = blockIdx.x * tilesPerCta, t1 = min(t0 + tilesPerCta, nTiles);
+    auto isLive = [&](int t) { return !live || live[t] != 0; };
+    {  // nothing to do when every instance of this CTA's tiles has stopped
+        bool any = false;
+        for (int t = t0; t < t1; t++) any = any || isLive(t);
+        if (!any) return;
+    }
+    auto prefetch = [&](int t) {
+        if (!isLive(t)) return;
+        T *sq = sBuf + (dbl ? ((t - t0) & 1) * bufElems : 0), *su = sq + nc * nx * kTileB, *sx = su + nu * kTileB;
+        const int bb = t * kTileB;
+        if (leafChildren)
+            gather(sq, nc * nx, cand, B, bb, lane, warp, [&](int r) { return D.oX + (long)c0 * nx + r; });
+        else
+            gather(sq, nc * nx, (const T *)Q, B, bb, lane, warp, [&](int r) { return (long)c0 * nx + r; });
+        gather(su, nu, cand, B, bb, lane, warp, [&](int r) { return (long)i * nu + r; });
+        if (stage > 0) gather(sx, nx, cand, B, bb, lane, warp, [&](int r) { return D.oX + (long)i * nx + r; });
+    };
+    if (t0 < t1) prefetch(t0);
+    cpAsyncCommit();
+    for (int tile = t0; tile < t1; tile++) {
+        if (dbl && tile + 1 < t1) prefetch(tile + 1);
+        cpAsyncCommit();
+        cpAsyncWaitPrev(dbl);
+        __syncthreads();
+        T *sq = sBuf + (dbl ? ((tile - t0) & 1) * bufElems : 0), *su = sq + nc * nx * kTileB, *sx = su + nu * kTileB;
+        const int b = tile * kTileB + lane;
+        const bool act = b < B;
+        auto tileBody = [&]() {
+        if (leafChildren || D.affine) {  // q of a leaf is -x; affine dynamics add P e (dynamics.cuh:96-99)
+            for (int t = warp; t < nc * nx; t += kTileWarps) {
+                T v = sq[t * kTileB + lane];
+                if (leafChildren) v = -v;
+                if (D.affine) v += P.Pe[(size_t)c0 * nx + t];
+                sq[t * kTileB + lane] = v;
+            }
+            __syncthreads();
+        }
+        T acc[kMaxTasks][kRT];
+        zeroAcc(acc);
+        for (int jj = 0; jj < nc; jj++) {
+            const T *qv = sq + jj * nx * kTileB + lane;
+            gemv(acc, sMat + jj * perChild, nu, nx, warp, [&](int k) { return qv[k * kTileB]; });
+        }
+#pragma unroll
+        for (int q = 0; q < kMaxTasks; q++) {
+            const int r0 = (warp + q * kTileWarps) * kRT;
+#pragma unroll
+            for (int t = 0; t < kRT; t++) {
+                const int r = r0 + t;
+                if (r < nu) sd[r * kTileB + lane] = su[r * kTileB + lane] - acc[q][t];
+            }
         }
         __syncthreads();
-    }
-    T acc[kMaxTasks][kRT];
-    zeroAcc(acc);
-    for (int jj = 0; jj < nc; jj++) {
-        const T *qv = sq + jj * nx * kTileB + lane;
-        gemv(acc, sMat + jj * perChild, nu, nx, warp, [&](int k) { return qv[k * kTileB]; });
-    }
-#pragma unroll
-    for (int q = 0; q < kMaxTasks; q++) {
-        const int r0 = (warp + q * kTileWarps) * kRT;
-#pragma unroll
-        for (int t = 0; t < kRT; t++) {
-            const int r = r0 + t;
-            if (r < nu) sd[r * kTileB + lane] = su[r * kTileB + lane] - acc[q][t];
+        if (warp == 0) {  // (I + sum B'PB) d = rhs with the cached lower Cholesky factor
+            const T *L = sL;  // padded: L(r, k) at k * ldu + r
+            T *v = sd + lane;
+            for (int r = 0; r < nu; r++) {
+                T s = v[r * kTileB];
+                for (int k = 0; k < r; k++) s -= L[k * ldu + r] * v[k * kTileB];
+                v[r * kTileB] = s / L[r * ldu + r];
+            }
+            for (int r = nu - 1; r >= 0; r--) {
+                T s = v[r * kTileB];
+                for (int k = r + 1; k < nu; k++) s -= L[r * ldu + k] * v[k * kTileB];
+                v[r * kTileB] = s / L[r * ldu + r];
+            }
         }
-    }
-    __syncthreads();
-    if (warp == 0) {  // (I + sum B'PB) d = rhs with the cached lower Cholesky factor
-        const T *L = sL;  // padded: L(r, k) at k * ldu + r
-        T *v = sd + lane;
-        for (int r = 0; r < nu; r++) {
-            T s = v[r * kTileB];
-            for (int k = 0; k < r; k++) s -= L[k * ldu + r] * v[k * kTileB];
-            v[r * kTileB] = s / L[r * ldu + r];
-        }
-        for (int r = nu - 1; r >= 0; r--) {
-            T s = v[r * kTileB];
-            for (int k = r + 1; k < nu; k++) s -= L[r * ldu + k] * v[k * kTileB];
-            v[r * kTileB] = s / L[r * ldu + r];
-        }
-    }
-    __syncthreads();
-    if (act)
-        for (int r = warp; r < nu; r += kTileWarps) DD[ix((long)i * nu + r, B, b)] = sd[r * kTileB + lane];
-    if (stage == 0) return;
-    zeroAcc(acc);
-    for (int jj = 0; jj < nc; jj++) {
-        const T *m = sMat + jj * perChild;
-        const T *qv = sq + jj * nx * kTileB + lane;
-        gemv(acc, m + ldu * nx, nx, nu, warp, [&](int k) { return sd[k * kTileB + lane]; });
-        gemv(acc, m + ldu * nx + ldx * nu, nx, nx, warp, [&](int k) { return qv[k * kTileB]; });
-    }
-    gemv(acc, sKt, nx, nu, warp,
-         [&](int k) { return sd[k * kTileB + lane] - su[k * kTileB + lane]; });
-    if (!act) return;
+        __syncthreads();
+        if (act)
+            for (int r = warp; r < nu; r += kTileWarps) DD[ix((long)i * nu + r, B, b)] = sd[r * kTileB + lane];
+        if (stage > 0) {
+            zeroAcc(acc);
+            for (int jj = 0; jj < nc; jj++) {
+                const T *m = sMat + jj * perChild;
+                const T *qv = sq + jj * nx * kTileB + lane;
+                gemv(acc, m + ldu * nx, nx, nu, warp, [&](int k) { return sd[k * kTileB + lane]; });
+                gemv(acc, m + ldu * nx + ldx * nu, nx, nx, warp, [&](int k) { return qv[k * kTileB]; });
+            }
+            gemv(acc, sKt, nx, nu, warp, [&](int k) { return sd[k * kTileB + lane] - su[k * kTileB + lane]; });
+            if (act) {
 #pragma unroll
-    for (int q = 0; q < kMaxTasks; q++) {
-        const int r0 = (warp + q * kTileWarps) * kRT;
+                for (int q = 0; q < kMaxTasks; q++) {
+                    const int r0 = (warp + q * kTileWarps) * kRT;
 #pragma unroll
-        for (int t = 0; t < kRT; t++) {
-            const int r = r0 + t;
-            if (r < nx) Q[ix((long)i * nx + r, B, b)] = acc[q][t] - sx[r * kTileB + lane];
+                    for (int t = 0; t < kRT; t++) {
+                        const int r = r0 + t;
+                        if (r < nx) Q[ix((long)i * nx + r, B, b)] = acc[q][t] - sx[r * kTileB + lane];
+                    }
+                }
+            }
         }
+        };
+        if (isLive(tile)) tileBody();
+        __syncthreads();  // sd and this tile's rows are reused by the next tile
+        if (!dbl && tile + 1 < t1) prefetch(tile + 1);
     }
 }
 
 // ------------------------------------------------------------------------------------------
 // Dynamics projection, one stage of the forward rollout (dynamics.cuh:143-173), writing the
-// candidate (x, u) and its residual Z - cand.
+// candidate (x, u) and its residual Z - cand.  Tiles as in k_dyn_back_b.
 // ------------------------------------------------------------------------------------------
 template <typename T>
 __global__ void __launch_bounds__(kTileB *kTileWarps) k_dyn_fwd_b(const DevProblem<T> P, const Dims D, const PadMats<T> M,
                                                                  T *__restrict__ cand, const T *__restrict__ DD,
                                                                  const T *__restrict__ x0s, int stageFrom,
-                                                                 const T *__restrict__ Z, T *__restrict__ R) {
+                                                                 const T *__restrict__ Z, T *__restrict__ R,
+                                                                 int tilesPerCta, int dbl, const int *live) {
     extern __shared__ __align__(16) unsigned char smraw[];
     T *sm = reinterpret_cast<T *>(smraw);
     const int B = D.B, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int b0 = blockIdx.x * kTileB, b = b0 + lane;
-    const bool act = b < B;
     const int i = stageFrom + blockIdx.y;
     const int nx = D.nx, nu = D.nu, nxu = D.nxu;
     const int c0 = P.chFrom[i], nc = P.numCh[i];
     const int ldx = pad16(nx), ldu = pad16(nu);
-    T *sK = sm, *sAB = sK + ldu * nx;
-    T *sxu = sAB + nc * ldx * nxu, *sdd = sxu + nxu * kTileB, *sz = sdd + nu * kTileB;  // sz: Z of [u_i][x_children][x_0]
+    const int nZ = nu + nc * nx + (i == 0 ? nx : 0);      // Z of [u_i][x_children][x_0]
+    const int bufElems = (nxu + nu + nZ) * kTileB;         // one tile's [x_i u_i], d_i and Z rows
+    T *sK = sm, *sAB = sK + ldu * nx, *sBuf = sAB + nc * ldx * nxu;
     stageMat(sK, M.K + (size_t)i * ldu * nx, ldu * nx);
     for (int jj = 0; jj < nc; jj++) stageMat(sAB + jj * ldx * nxu, M.AB + (size_t)(c0 + jj) * ldx * nxu, ldx * nxu);
-    const int nZ = nu + nc * nx + (i == 0 ? nx : 0);
-    if (i == 0) gather(sxu, nx, x0s, B, b0, lane, warp, [&](int r) { return (long)r; });
-    else gather(sxu, nx, (const T *)cand, B, b0, lane, warp, [&](int r) { return D.oX + (long)i * nx + r; });
-    gather(sdd, nu, DD, B, b0, lane, warp, [&](int r) { return (long)i * nu + r; });
-    if (R)
-        gather(sz, nZ, Z, B, b0, lane, warp, [&](int r) -> long {
-            if (r < nu) return (long)i * nu + r;
-            if (r < nu + nc * nx) return D.oX + (long)c0 * nx + (r - nu);
-            return D.oX + (r - nu - nc * nx);
-        });
-    cpAsyncWaitAll();
-    __syncthreads();
-    if (i == 0 && act)
-        for (int r = warp; r < nx; r += kTileWarps) {
-            const T x = sxu[r * kTileB + lane];
-            cand[ix(D.oX + r, B, b)] = x;
-            if (R) R[ix(D.oX + r, B, b)] = sz[(nu + nc * nx + r) * kTileB + lane] - x;
-        }
-    T acc[kMaxTasks][kRT];
-    zeroAcc(acc);
-    gemv(acc, sK, nu, nx, warp, [&](int k) { return sxu[k * kTileB + lane]; });
-    __syncthreads();  // every warp has read x before u is appended
-#pragma unroll
-    for (int q = 0; q < kMaxTasks; q++) {
-        const int r0 = (warp + q * kTileWarps) * kRT;
-#pragma unroll
-        for (int t = 0; t < kRT; t++) {
-            const int r = r0 + t;
-            if (r < nu) {
-                const T u = acc[q][t] + sdd[r * kTileB + lane];
-                sxu[(nx + r) * kTileB + lane] = u;
-                if (act) {
-                    cand[ix((long)i * nu + r, B, b)] = u;
-                    if (R) R[ix((long)i * nu + r, B, b)] = sz[r * kTileB + lane] - u;
-                }
-            }
-        }
+    const int nTiles = (B + kTileB - 1) / kTileB;
+    const int t0 = blockIdx.x * tilesPerCta, t1 = min(t0 + tilesPerCta, nTiles);
+    auto isLive = [&](int t) { return !live || live[t] != 0; };
+    {  // nothing to do when every instance of this CTA's tiles has stopped
+        bool any = false;
+        for (int t = t0; t < t1; t++) any = any || isLive(t);
+        if (!any) return;
     }
-    __syncthreads();
-    for (int jj = 0; jj < nc; jj++) {
-        const int j = c0 + jj;
+    auto prefetch = [&](int t) {
+        if (!isLive(t)) return;
+        T *sxu = sBuf + (dbl ? ((t - t0) & 1) * bufElems : 0), *sdd = sxu + nxu * kTileB, *sz = sdd + nu * kTileB;
+        const int bb = t * kTileB;
+        if (i == 0) gather(sxu, nx, x0s, B, bb, lane, warp, [&](int r) { return (long)r; });
+        else gather(sxu, nx, (const T *)cand, B, bb, lane, warp, [&](int r) { return D.oX + (long)i * nx + r; });
+        gather(sdd, nu, DD, B, bb, lane, warp, [&](int r) { return (long)i * nu + r; });
+        if (R)
+            gather(sz, nZ, Z, B, bb, lane, warp, [&](int r) -> long {
+                if (r < nu) return (long)i * nu + r;
+                if (r < nu + nc * nx) return D.oX + (long)c0 * nx + (r - nu);
+                return D.oX + (r - nu - nc * nx);
+            });
+    };
+    if (t0 < t1) prefetch(t0);
+    cpAsyncCommit();
+    for (int tile = t0; tile < t1; tile++) {
+        if (dbl && tile + 1 < t1) prefetch(tile + 1);
+        cpAsyncCommit();
+        cpAsyncWaitPrev(dbl);
+        __syncthreads();
+        T *sxu = sBuf + (dbl ? ((tile - t0) & 1) * bufElems : 0), *sdd = sxu + nxu * kTileB, *sz = sdd + nu * kTileB;
+        const int b = tile * kTileB + lane;
+        const bool act = b < B;
+        auto tileBody = [&]() {
+        if (i == 0 && act)
+            for (int r = warp; r < nx; r += kTileWarps) {
+                const T x = sxu[r * kTileB + lane];
+                cand[ix(D.oX + r, B, b)] = x;
+                if (R) R[ix(D.oX + r, B, b)] = sz[(nu + nc * nx + r) * kTileB + lane] - x;
+            }
+        T acc[kMaxTasks][kRT];
         zeroAcc(acc);
-        const int slot = slotFrom(warp, jj * tasksOf(nx));  // children's blocks on different warps
-        gemv(acc, sAB + jj * ldx * nxu, nx, nxu, slot, [&](int k) { return sxu[k * kTileB + lane]; });
-        if (!act) continue;
+        gemv(acc, sK, nu, nx, warp, [&](int k) { return sxu[k * kTileB + lane]; });
 #pragma unroll
         for (int q = 0; q < kMaxTasks; q++) {
-            const int r0 = (slot + q * kTileWarps) * kRT;
+            const int r0 = (warp + q * kTileWarps) * kRT;
 #pragma unroll
             for (int t = 0; t < kRT; t++) {
                 const int r = r0 + t;
-                if (r < nx) {
-                    const T x = acc[q][t] + (D.affine ? P.e[(size_t)j * nx + r] : T(0));
-                    cand[ix(D.oX + (long)j * nx + r, B, b)] = x;
-                    if (R) R[ix(D.oX + (long)j * nx + r, B, b)] = sz[(nu + jj * nx + r) * kTileB + lane] - x;
+                if (r < nu) {
+                    const T u = acc[q][t] + sdd[r * kTileB + lane];
+                    sxu[(nx + r) * kTileB + lane] = u;
+                    if (act) {
+                        cand[ix((long)i * nu + r, B, b)] = u;
+                        if (R) R[ix((long)i * nu + r, B, b)] = sz[r * kTileB + lane] - u;
+                    }
                 }
             }
         }
+        __syncthreads();  // u is complete before the children read [x; u]
+        for (int jj = 0; jj < nc; jj++) {
+            const int j = c0 + jj;
+            zeroAcc(acc);
+            const int slot = slotFrom(warp, jj * tasksOf(nx));  // children's blocks on different warps
+            gemv(acc, sAB + jj * ldx * nxu, nx, nxu, slot, [&](int k) { return sxu[k * kTileB + lane]; });
+            if (!act) continue;
+#pragma unroll
+            for (int q = 0; q < kMaxTasks; q++) {
+                const int r0 = (slot + q * kTileWarps) * kRT;
+#pragma unroll
+                for (int t = 0; t < kRT; t++) {
+                    const int r = r0 + t;
+                    if (r < nx) {
+                        const T x = acc[q][t] + (D.affine ? P.e[(size_t)j * nx + r] : T(0));
+                        cand[ix(D.oX + (long)j * nx + r, B, b)] = x;
+                        if (R) R[ix(D.oX + (long)j * nx + r, B, b)] = sz[(nu + jj * nx + r) * kTileB + lane] - x;
+                    }
+                }
+            }
+        }
+        };
+        if (isLive(tile)) tileBody();
+        __syncthreads();  // this tile's rows are reused by the next tile
+        if (!dbl && tile + 1 < t1) prefetch(tile + 1);
     }
 }
 

@@ -72,6 +72,9 @@ _SIGS = {
     "spock_round_time": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
     "spock_run_stats": (ctypes.c_int, [_vp, _lp, _lp]),
     "spock_tuning": (ctypes.c_int, [_vp, _ip]),
+    "spock_counters_all": (ctypes.c_int, [_vp, _lp]),
+    "spock_copy_iterate": (ctypes.c_int, [_vp, _vp]),
+    "spock_offline_dynamics": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp, _dp]),
     "spock_resolve": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.c_long, _ip, _lp]),
     "spock_resolve_device": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _ip, _lp]),
     "spock_project_dynamics_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
@@ -138,6 +141,18 @@ class ScenarioTree:
             self._h = None
 
     def path(self): return self._path
+
+    def offlineDynamics(self, device=0, replace=False):
+        """The dynamics projection's offline cache (problem.py:192-213) recomputed on the GPU in
+        FP64 from this problem's [A B]: dict of P, K, lowChol, ABKTr, APB in the .bt layouts.
+        With replace=True solvers created afterwards use it."""
+        n, nnl, nx, nu = self._n, self._nnl, self._nx, self._nu
+        out = {"P": np.zeros(nx * nx * n), "K": np.zeros(nu * nx * nnl), "lowChol": np.zeros(nu * nu * nnl),
+               "ABKTr": np.zeros(nx * nx * n), "APB": np.zeros(nx * nu * n)}
+        _check(lib().spock_offline_dynamics(self._h, device, int(replace), _p(out["P"]), _p(out["K"]),
+                                            _p(out["lowChol"]), _p(out["ABKTr"]), _p(out["APB"])))
+        return out
+
     def numEvents(self): return self._ne
     def numNodes(self): return self._n
     def numNonleafNodes(self): return self._nnl
@@ -277,6 +292,17 @@ class Cache:
                                           self._status.ctypes.data_as(_ip), self._iters.ctypes.data_as(_lp)))
         return self._status.copy()
 
+    def copyIterateFrom(self, other):
+        """Take another solver's current iterate (same problem and batch, same GPU), converted to
+        this solver's precision on the device."""
+        _check(lib().spock_copy_iterate(self._h, other._h))
+
+    def polish(self, fp32_solver, x0s):
+        """FP64 polish: continue from `fp32_solver`'s solution under this (FP64) solver's
+        tolerances, with the same initial states.  Returns the status array."""
+        self.copyIterateFrom(fp32_solver)
+        return self.resolveBatch(x0s)
+
     def status(self, instance=0): return int(self._status[instance])
     def statuses(self): return self._status.copy()
     def solveIter(self, instance=0): return int(self._iters[instance])
@@ -320,6 +346,12 @@ class Cache:
         _check(lib().spock_counters(self._h, out.ctypes.data_as(_lp)))
         return dict(zip(["K0", "K1", "K2", "bt", "K3", "calls_T", "iters"], out.tolist()))
 
+    def countersAll(self):
+        """Per-instance counters, a (batch, 7) array: K0, K1, K2, backtracks, K3, T calls, iterations."""
+        out = np.zeros((self._B, 7), dtype=np.int64)
+        _check(lib().spock_counters_all(self._h, out.ctypes.data_as(_lp)))
+        return out
+
     def reset(self):
         _check(lib().spock_reset(self._h))
         self._status[:] = NOT_RUN
@@ -361,11 +393,11 @@ class Cache:
         return ms.value, b.value
 
     def tuning(self):
-        """Tile shapes chosen by the autotuner for L* and L (runs it if needed)."""
+        """Tile shapes chosen by the autotuner for L*, L and the dynamics sweep (runs it if needed)."""
         out = np.zeros(5, dtype=np.int32)
         _check(lib().spock_tuning(self._h, out.ctypes.data_as(_ip)))
         return dict(zip(["lstar_tiles_per_cta", "lstar_double_buffer", "lop_tiles_per_cta", "lop_double_buffer",
-                         "batched_kernels"], out.tolist()))
+                         "dyn_tiles_per_cta"], out.tolist()))
 
     def runStats(self):
         """(rounds, kernel launches) of the last solve."""

@@ -189,12 +189,30 @@ def test_warm_start_from_solution(oracle_lib):
     assert c.solveIter() <= it_cold
 
 
-def test_unsupported_types_fail_loudly():
-    path = os.path.join(GOLDEN, "affpoly")
-    t = sg.ScenarioTree(path)
-    d = sg.ProblemData(t)
-    with pytest.raises(ValueError, match="not supported"):
-        sg.CacheBuilder(t, d).build()
+@pytest.mark.parametrize("batch", [1, 32])
+@pytest.mark.parametrize("precision,tol", [(64, 1e-12), (32, 2e-5)])
+def test_linear_costs_polyhedra_affine(oracle_lib, batch, precision, tol):
+    """Affine dynamics, linear costs and polyhedral constraints (the reference factory's affpoly
+    fixture): L and L* against the reference's own vectors, one CP step from random iterates
+    against the oracle, and 200 plain CP iterations taking the oracle's path (FP64)."""
+    case = "affpoly"
+    path = os.path.join(GOLDEN, case)
+    t, d, c = make(path, precision, batch=batch)
+    P = oracle_lib.Problem(path)
+    prim = golden(case, "test_primBeforeOp_d.bt")
+    dual = golden(case, "test_dualAfterOpBeforeAdj_d.bt")
+    assert rel(c.op(prim), dual) < tol
+    assert rel(c.adj(dual), golden(case, "test_primAfterAdj_d.bt")) < tol
+    rng = np.random.default_rng(31)
+    x0 = rng.uniform(-1, 1, P.nx)
+    for _ in range(3):
+        z = 3 * rng.standard_normal(P.size)
+        assert rel(c.cpStep(x0, z), P.cp_step(x0, z)) < (1e-10 if precision == 64 else 1e-4)
+    if precision == 64:
+        t2, d2, c2 = make(path, 64, batch=batch, tol=1e-12, max_iters=200)
+        c2.runCp(x0)
+        z, s = P.run(x0, oracle_lib.options(tol=1e-12, max_iters=200), "cp")
+        assert rel(c2.solution(), z) < 1e-8
 
 
 @pytest.mark.parametrize("batch", BATCHES)
@@ -237,3 +255,71 @@ def test_full_size_dynamics_feasible(oracle_lib, tmp_problems, batch):
     assert np.allclose(x[0], x0[0] * P.scaling[:nx], atol=1e-6)
     pred = np.einsum("rcn,nc->nr", AB[:, :, 1:], np.concatenate((x[anc[1:]], u[anc[1:]]), axis=1))
     assert np.abs(pred - x[1:]).max() <= 1e-4 * max(1., np.abs(x).max())
+
+
+def test_resolve_from_previous_solution(oracle_lib):
+    """spock_resolve: 64 cfg1 instances re-solved warm from their previous solutions after a small
+    move of x0 (the previousSolution path, cache.cuh:611-632, kept on the device) converge, and
+    their first inputs agree with cold solves of the same states."""
+    path = os.path.join(GOLDEN, "cfg1")
+    P = oracle_lib.Problem(path)
+    rng = np.random.default_rng(21)
+    x0s = rng.uniform(-1, 1, (64, P.nx))
+    # a warm start captures a small initial error, so the absolute tolerance decides: FP64 and a
+    # generous cap keep the slowest instances inside it
+    t, d, c = make(path, 64, batch=64, tol=1e-3, max_iters=20000)
+    assert (c.runSpockBatch(x0s) == 0).all()
+    x1 = x0s + rng.uniform(-.05, .05, x0s.shape)
+    assert (c.resolveBatch(x1) == 0).all()
+    u_warm = c.firstInputs()
+    t2, d2, c2 = make(path, 64, batch=64, tol=1e-3, max_iters=20000)
+    assert (c2.runSpockBatch(x1) == 0).all()
+    assert np.abs(u_warm - c2.firstInputs()).max() <= 2e-2 * max(1., np.abs(c2.firstInputs()).max())
+
+
+def test_converged_instances_stay_put(oracle_lib):
+    """Per-instance convergence masks: in a batch whose instances stop at very different
+    iterations (half of them start at their own solution), the early ones keep the solution they
+    stopped at while the node kernels skip their tiles."""
+    path = os.path.join(GOLDEN, "cfg1")
+    P = oracle_lib.Problem(path)
+    rng = np.random.default_rng(22)
+    x0s = rng.uniform(-1, 1, (64, P.nx))
+    t, d, c = make(path, 64, batch=64, tol=1e-6, max_iters=5000)
+    assert (c.runSpockBatch(x0s) == 0).all()
+    z = c.solutions()
+    warm = z.copy()
+    warm[32:] = 0.  # tiles 0 (warm, stop early) and 1 (cold, run long)
+    assert (c.runSpockBatch(x0s, prev=warm) == 0).all()
+    it = c.solveIters()
+    assert it[:32].max() < it[32:].min()
+    assert np.abs(c.solutions()[:32] - z[:32]).max() <= 1e-5 * max(1., np.abs(z).max())
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_offline_dynamics_cache_on_gpu(case):
+    """spock_offline_dynamics: the dynamics cache (problem.py:192-213) recomputed on the GPU in
+    FP64 matches the reference factory's own files to 1e-10 relative."""
+    t = sg.ScenarioTree(os.path.join(GOLDEN, case))
+    out = t.offlineDynamics(replace=False)
+    for name, key in [("P", "P"), ("K", "K"), ("lowCholesky", "lowChol"), ("ABKTr", "ABKTr"), ("APB", "APB")]:
+        ref = golden(case, f"dynamics_{name}_d.bt")
+        assert np.abs(out[key] - ref).max() <= 1e-10 * max(1., np.abs(ref).max()), name
+
+
+def test_fp64_polish_of_fp32_solve(oracle_lib):
+    """FP32 batch solve to 1e-3, handed over on the device to an FP64 solver that polishes to
+    1e-9 (spock_copy_iterate + spock_resolve): every instance converges and u_0 agrees with the
+    oracle's FP64 solve at 1e-9 to 1e-6."""
+    path = os.path.join(GOLDEN, "reftest")
+    P = oracle_lib.Problem(path)
+    x0s = np.full((32, P.nx), 1.1) + np.linspace(-.05, .05, 32)[:, None]
+    t, d, c32 = make(path, 32, batch=32, tol=1e-3, max_iters=20000)
+    assert (c32.runSpockBatch(x0s) == 0).all()
+    t2, d2, c64 = make(path, 64, batch=32, tol=1e-9, max_iters=20000)
+    assert (c64.polish(c32, x0s) == 0).all()
+    u0 = c64.firstInputs()
+    for b in (0, 31):
+        z, s = P.run(x0s[b], oracle_lib.options(tol=1e-9, max_iters=20000), "spock")
+        u_ref = P.states_inputs(z)[1][:P.nu]
+        assert np.abs(u0[b] - u_ref).max() <= 1e-6 * max(1., np.abs(u_ref).max()), b
