@@ -132,9 +132,9 @@ int spock_apply_m(spock_solver s, const double *z, double *mz);            /* M 
  * algorithmic bytes, and the device time of `rounds` replays of the captured SuperMann round. */
 int spock_kernel_time(spock_solver s, const char *which, int reps, double *ms, long *bytes);
 int spock_round_time(spock_solver s, int rounds, double *ms);
-/* Rounds (one T evaluation + one M application per instance each) and kernel launches of the
- * last solve. */
-int spock_run_stats(spock_solver s, long *rounds, long *launches);
+/* Rounds (one T evaluation + one M application per instance each), kernel launches and instance
+ * compactions (running instances moved to the leading slots) of the last solve; NULL skips one. */
+int spock_run_stats(spock_solver s, long *rounds, long *launches, long *compactions);
 /* Tile shapes the built-in autotuner chose (it times 1, 2, 4 and 8 instance tiles per CTA once,
  * before the first solve): out5 = {L* tiles per CTA, L* double-buffered, L tiles per CTA, L
  * double-buffered, dynamics-sweep tiles per CTA (0 when the small-batch kernels run)}.  No

@@ -27,7 +27,9 @@
 #include <time.h>
 
 enum { COST_QUAD = 0, COST_LIN = 1, COST_QPL = 2 };
-enum { CON_NO = 0, CON_RECT = 1, CON_POLY = 2, CON_POLYID = 3 };
+/* CON_RECTBALL (nonleaf only, no counterpart in the reference): a box on [x; u] with infinite
+ * input bounds, plus ||u||_2 <= radius at every nonleaf node. */
+enum { CON_NO = 0, CON_RECT = 1, CON_POLY = 2, CON_POLYID = 3, CON_RECTBALL = 4 };
 
 struct OrProblem {
     long ne, n, nnl, nl, ns, nx, nu, nxu;
@@ -35,6 +37,7 @@ struct OrProblem {
     double *prob, *cprob;
     int affine, costNl, costL, conNl, conL, precond;
     double alpha, step;
+    double nlRadius; /* CON_RECTBALL */
     double *scaling;
     long nullDim, yDim;
     /* dynamics (per node) */
@@ -161,6 +164,7 @@ static int parse_con(const char *s) {
     if (!strcmp(s, "rectangle")) return CON_RECT;
     if (!strcmp(s, "polyhedron")) return CON_POLY;
     if (!strcmp(s, "polyhedronWithIdentity")) return CON_POLYID;
+    if (!strcmp(s, "rectangleInputBall")) return CON_RECTBALL;
     return -1;
 }
 
@@ -189,6 +193,15 @@ static int load_constraint(OrProblem *p, const char *dir, int leaf, int type, lo
     *size = 0;
     *lbOut = *ubOut = *gOut = NULL;
     if (type == CON_NO) return 0;
+    if (type == CON_RECTBALL) {
+        double *rad = NULL;
+        if (leaf) return -1;
+        snprintf(nm, sizeof nm, "%sRadius", part);
+        if (read_bt(dir, nm, 'd', (void **)&rad, dims) != 1) return -1;
+        p->nlRadius = rad[0];
+        free(rad);
+        type = CON_RECT; /* bounds exactly as a rectangle */
+    }
     if (type == CON_RECT || type == CON_POLYID) {
         snprintf(nm, sizeof nm, "%sILB", part);
         if (read_bt(dir, nm, 'd', (void **)&ilb, dims) != dpn) return -1;
@@ -430,7 +443,7 @@ void or_op(const OrProblem *p, const double *prim, double *dual) {
     for (long i = 0; i < nnl && p->conNl != CON_NO; i++) {
         memcpy(xu, x + i * nx, sizeof(double) * (size_t)nx);
         memcpy(xu + nx, u + i * nu, sizeof(double) * (size_t)nu);
-        if (p->conNl == CON_RECT) memcpy(III + i * nxu, xu, sizeof(double) * (size_t)nxu);
+        if (p->conNl == CON_RECT || p->conNl == CON_RECTBALL) memcpy(III + i * nxu, xu, sizeof(double) * (size_t)nxu);
         else if (p->conNl == CON_POLY) matvec(p->nlGamma, p->nlGRows, nxu, xu, III + i * p->nlGRows, 0);
         else {
             memcpy(III + i * nxu, xu, sizeof(double) * (size_t)nxu);
@@ -491,7 +504,7 @@ void or_adj(const OrProblem *p, const double *dual, double *prim) {
         for (long k = 0; k < yD; k++) y[i * yD + k] = I[i * yD + k] - p->b[i * yD + k] * II[i];
     }
     for (long i = 0; i < nnl && p->conNl != CON_NO; i++) {
-        if (p->conNl == CON_RECT) memcpy(xu, III + i * nxu, sizeof(double) * (size_t)nxu);
+        if (p->conNl == CON_RECT || p->conNl == CON_RECTBALL) memcpy(xu, III + i * nxu, sizeof(double) * (size_t)nxu);
         else if (p->conNl == CON_POLY) matTvec(p->nlGamma, p->nlGRows, nxu, III + i * p->nlGRows, xu, 0);
         else {
             memcpy(xu, III + i * nxu, sizeof(double) * (size_t)nxu);
@@ -676,6 +689,13 @@ void or_project_dual(const OrProblem *p, double *dual) {
     }
     for (long i = 0; i < p->nnl; i++) II[i] = fmax(0., II[i]);
     if (p->sIII) or_project_box(dual + p->oIII, p->nlLb, p->nlUb, p->sIII);
+    if (p->conNl == CON_RECTBALL) /* ||u|| <= radius: u * min(1, radius / ||u||) */
+        for (long i = 0; i < p->nnl; i++) {
+            double *u = dual + p->oIII + i * p->nxu + p->nx;
+            const double nrm = sqrt(dotv(u, u, p->nu));
+            if (nrm > p->nlRadius)
+                for (long k = 0; k < p->nu; k++) u[k] *= p->nlRadius / nrm;
+        }
     if (p->costNl == COST_LIN) project_linear_epi(dual + p->oIV, p->n);
     else or_project_soc_columns(dual + p->oIV, p->nxu + 2, p->n);
     if (p->sV) or_project_box(dual + p->oV, p->lLb, p->lUb, p->sV);

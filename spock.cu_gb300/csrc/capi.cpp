@@ -354,11 +354,12 @@ int spock_round_time(spock_solver sv, int rounds, double *ms) {
     });
 }
 
-int spock_run_stats(spock_solver sv, long *rounds, long *launches) {
+int spock_run_stats(spock_solver sv, long *rounds, long *launches, long *compactions) {
     return guard([&] {
         auto *s = solver(sv);
         if (rounds) *rounds = s->eng->lastRounds();
         if (launches) *launches = s->eng->lastLaunches();
+        if (compactions) *compactions = s->eng->lastCompactions();
     });
 }
 

@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce(const Dims Dm, const Red
                 const double x = sred[(v * lanes + l) * TB + lb];
                 s = (v == 1) ? fmax(s, x) : s + x;
             }
-            A.part[((size_t)chunk * A.nv + v) * B + b] = s;
+            A.part[((size_t)b * A.nv + v) * A.chunks + chunk] = s;  // [instance][value][chunk]
         }
 }
 
@@ -156,23 +156,9 @@ __device__ bool solveGram(const double *G, const double *h, int m, double ridge,
     return true;
 }
 
-__global__ void k_control(const int B, const CtlArgs A) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= B) return;
+// The SuperMann / CP decision of instance b from its reduced values v (see k_control).
+__device__ void controlInstance(const CtlArgs &A, const int b, const double *v) {
     const DevState &S = A.S;
-    if (S.status[b] != -1) {
-        S.action[b] = kActNone;
-        return;
-    }
-    double v[kNV0 + 2 * kMaxAnderson];
-    for (int k = 0; k < A.nv; k++) {
-        double s = 0;
-        for (int c = 0; c < A.chunks; c++) {
-            const double x = A.part[((size_t)c * A.nv + k) * B + b];
-            s = (k == 1) ? fmax(s, x) : s + x;
-        }
-        v[k] = s;
-    }
     const double c0 = .99, c1 = .99, c2 = .99, beta = .5, sigma = .1, lambda = 1.;
     const int m = A.m;
     // error check (cache.cuh:909-961): r/gamma - [L* r_d; L r_p] = (M r)/gamma
@@ -277,6 +263,35 @@ __global__ void k_control(const int B, const CtlArgs A) {
     S.action[b] = kActBBt;
 }
 
+// One warp per instance: the lanes reduce the chunk partials of the 21 values (sums, and a
+// maximum for max|Mr|) with shuffles, then lane 0 takes the instance's decision.
+__global__ void k_control(const int B, const CtlArgs A) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int b = blockIdx.x * (blockDim.x >> 5) + warp;
+    if (b >= B) return;  // the whole warp
+    if (A.S.status[b] != -1) {
+        if (lane == 0) A.S.action[b] = kActNone;
+        return;
+    }
+    double v[kNV0 + 2 * kMaxAnderson];
+#pragma unroll
+    for (int k = 0; k < kNV0 + 2 * kMaxAnderson; k++) {
+        double s = 0;
+        if (k < A.nv)
+            for (int c = lane; c < A.chunks; c += 32) {
+                const double x = A.part[((size_t)b * A.nv + k) * A.chunks + c];
+                s = (k == 1) ? fmax(s, x) : s + x;
+            }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double y = __shfl_xor_sync(0xffffffffu, s, o);
+            s = (k == 1) ? fmax(s, y) : s + y;
+        }
+        v[k] = s;
+    }
+    if (lane == 0) controlInstance(A, b, v);
+}
+
 // ------------------------------------------------------------------------------------------ vector update
 template <typename T>
 struct UpdArgs {
@@ -335,77 +350,6 @@ __global__ void __launch_bounds__(256) k_update(const Dims Dm, const UpdArgs<T> 
     }
 }
 
-// The same update for batches of >= 32 instances, one thread per (instance, row subset): lane b
-// reads its action once and streams rows k of a chunk with stride 8 (the warps of the block), so
-// every warp access is one 128-byte row segment of 32 instances, with no per-element index
-// arithmetic or branch.
-template <typename T>
-__global__ void __launch_bounds__(256) k_update_b(const Dims Dm, const UpdArgs<T> A, long rowsPerChunk) {
-    const int B = Dm.B;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int b = blockIdx.x * 32 + lane;
-    if (b >= B) return;
-    const long k0 = (long)blockIdx.y * rowsPerChunk;
-    const long k1 = k0 + rowsPerChunk < Dm.sZ ? k0 + rowsPerChunk : Dm.sZ;
-    const size_t slot = (size_t)Dm.sZ * B;
-    switch (A.action[b]) {
-        case kActAK0:
-        case kActALs: {
-            const int m = A.m;
-            const int h = (A.head[b] + m - 1) % m;  // slot written this round (head already advanced)
-            const bool useAnd = A.useAnd[b];
-            T g[kMaxAnderson];
-#pragma unroll
-            for (int s2 = 0; s2 < kMaxAnderson; s2++)
-                g[s2] = (useAnd && s2 < m) ? T(A.gamma[(size_t)b * kMaxAnderson + s2]) : T(0);
-            for (long k = k0 + warp; k < k1; k += 8) {
-                const size_t o = (size_t)k * B + b;
-                const T z = A.Z[o], r = A.R[o], c = A.CAND[o];
-                const T dr = r - A.RPREV[o];
-                const T dzr = (z - A.PREV[o]) - dr;
-                T d = -r;
-                if (useAnd)
-#pragma unroll
-                    for (int s2 = 0; s2 < kMaxAnderson; s2++)
-                        if (s2 < m) d -= g[s2] * (s2 == h ? dzr : A.ANDZ[s2 * slot + o]);
-                A.ANDR[h * slot + o] = dr;
-                A.ANDZ[h * slot + o] = dzr;
-                A.D[o] = d;
-                A.PREV[o] = z;
-                A.RPREV[o] = r;
-                A.BACKUP[o] = c;
-                A.Z[o] = z + d;
-            }
-            break;
-        }
-        case kActFinish:
-        case kActCp:
-            for (long k = k0 + warp; k < k1; k += 8) A.Z[(size_t)k * B + b] = A.CAND[(size_t)k * B + b];
-            break;
-        case kActBK2: {
-            const T cf = T(A.coef[b]);
-            for (long k = k0 + warp; k < k1; k += 8) {
-                const size_t o = (size_t)k * B + b;
-                A.Z[o] = A.PREV[o] - cf * A.R[o];
-            }
-            break;
-        }
-        case kActBK3:
-            for (long k = k0 + warp; k < k1; k += 8) A.Z[(size_t)k * B + b] = A.BACKUP[(size_t)k * B + b];
-            break;
-        case kActBBt: {
-            const T tau = T(A.tau[b]);
-            for (long k = k0 + warp; k < k1; k += 8) {
-                const size_t o = (size_t)k * B + b;
-                A.Z[o] = A.PREV[o] + tau * A.D[o];
-            }
-            break;
-        }
-        default:
-            break;
-    }
-}
-
 // ------------------------------------------------------------------------------------------ small kernels
 template <typename T>
 __global__ void k_fill(T *p, size_t n, T v) {
@@ -442,6 +386,32 @@ __global__ void k_init_state(DevState S, int B, int warm) {
     for (int k = 0; k < kMaxAnderson * kMaxAnderson; k++) S.G[(size_t)b * kMaxAnderson * kMaxAnderson + k] = 0;
     for (int k = 0; k < kMaxAnderson; k++) S.gamma[(size_t)b * kMaxAnderson + k] = 0;
     if (b == 0) { *S.timeUp = 0; }
+}
+
+// Instance compaction.  dst[k * B + s] = src[k * B + from[s]] for rows k of an element-major
+// buffer: slot s receives the column of slot from[s].
+template <typename T>
+__global__ void k_gather_cols(T *__restrict__ dst, const T *__restrict__ src, const int *__restrict__ from, long rows,
+                              int B) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= B) return;
+    const int f = from[s];
+    for (long k = blockIdx.y; k < rows; k += gridDim.y) dst[(size_t)k * B + s] = src[(size_t)k * B + f];
+}
+
+// The controller state of slot s from slot from[s]: nInt int fields and nDbl double fields laid out
+// [field][instance], then the m x m Gram matrices and the Anderson coefficients per instance.
+__global__ void k_gather_state(int *__restrict__ id, const int *__restrict__ is, double *__restrict__ dd,
+                               const double *__restrict__ ds, const int *__restrict__ from, int B, int nInt, int nDbl,
+                               int perG, int perGamma) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= B) return;
+    const int f = from[s];
+    for (int q = 0; q < nInt; q++) id[(size_t)q * B + s] = is[(size_t)q * B + f];
+    for (int q = 0; q < nDbl; q++) dd[(size_t)q * B + s] = ds[(size_t)q * B + f];
+    const size_t g0 = (size_t)nDbl * B, a0 = g0 + (size_t)perG * B;
+    for (int q = 0; q < perG; q++) dd[g0 + (size_t)s * perG + q] = ds[g0 + (size_t)f * perG + q];
+    for (int q = 0; q < perGamma; q++) dd[a0 + (size_t)s * perGamma + q] = ds[a0 + (size_t)f * perGamma + q];
 }
 
 // Measurement helper: put every instance in phase A with an Anderson update pending.
@@ -568,6 +538,8 @@ public:
         k_init_state<<<((int)B_ + 127) / 128, 128, 0, stream_>>>(S_, (int)B_, warm ? 1 : 0);
         CK(cudaGetLastError());
         allLive();
+        capacity_ = B_;
+        compactions_ = 0;
         int rounds = 0, polls = 0;
         long launches = (algo == kSpock ? 5 : 2) + 2;  // buffer fills + state init + tile flags
         const int poll = B_ > 1 ? 10 : 25;
@@ -579,9 +551,12 @@ public:
                 launches += launchesPerRound();
                 if (rounds % poll == 0) {
                     polls++;
-                    if (activeCount(t0) == 0) break;
+                    const int act = activeCount(t0);
+                    if (act == 0) break;
+                    maybeCompact(act);
                 }
             }
+            restoreOrder();
         } else {
             for (;;) {
                 teval();
@@ -600,6 +575,7 @@ public:
             }
         }
         lastRounds_ = rounds;
+        lastCompactions_ = compactions_;
         lastLaunches_ = launches + polls;
         CK(cudaStreamSynchronize(stream_));
         lastSeconds_ = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -818,6 +794,12 @@ private:
     T *Z_ = nullptr, *CAND_ = nullptr, *R_ = nullptr, *MR_ = nullptr, *PREV_ = nullptr, *RPREV_ = nullptr;
     T *BACKUP_ = nullptr, *DIR_ = nullptr, *ANDR_ = nullptr, *ANDZ_ = nullptr, *Q_ = nullptr, *DD_ = nullptr;
     T *x0s_ = nullptr, *W1_ = nullptr, *W2_ = nullptr, *scal_ = nullptr;
+    // instance compaction: slot s holds instance slotInst_[s]; state blocks and their copies
+    int *ib_ = nullptr, *ibTmp_ = nullptr, *from_ = nullptr;
+    double *db_ = nullptr, *dbTmp_ = nullptr;
+    std::vector<int> slotInst_;
+    long capacity_ = 0;  // slots in live tiles after the last compaction
+    int compactions_ = 0;
     double *part_ = nullptr;
     int *hostActive_ = nullptr, *devActive_ = nullptr;
     int chunks_ = 1, nv_ = 0;
@@ -888,6 +870,7 @@ private:
         P_.nlLo = upvec<T>(p.nlLower); P_.nlHi = upvec<T>(p.nlUpper); P_.lLo = upvec<T>(p.lLower); P_.lHi = upvec<T>(p.lUpper);
         P_.NNtr = upvec<T>(p.NNtr); P_.b = upvec<T>(p.b);
         P_.grad = upvec<T>(p.gradient); P_.lGrad = upvec<T>(p.leafGradient);
+        P_.radius = (T)p.nlRadius;
         P_.step = (T)p.stepSize;
         scal_ = const_cast<T *>(upvec<T>(p.scaling));
     }
@@ -916,13 +899,18 @@ private:
     // L* and L stage the node's matrices once and one (or, double-buffered, two) instance
     // tiles of input and base rows.
     // rows of the constraint blocks: identity part and Gamma part (nonleaf, leaf)
-    int idNl() const { return (D_.conNl == kConRectangle || D_.conNl == kConPolyhedronWithIdentity) ? D_.nxu : 0; }
+    int idNl() const {
+        return (D_.conNl == kConRectangle || D_.conNl == kConPolyhedronWithIdentity || D_.conNl == kConRectangleInputBall)
+                   ? D_.nxu
+                   : 0;
+    }
     int idL() const { return (D_.conL == kConRectangle || D_.conL == kConPolyhedronWithIdentity) ? D_.nx : 0; }
     int gNl() const { return (D_.conNl == kConPolyhedron || D_.conNl == kConPolyhedronWithIdentity) ? D_.gNl : 0; }
     int gL() const { return (D_.conL == kConPolyhedron || D_.conL == kConPolyhedronWithIdentity) ? D_.gL : 0; }
     bool needsBatched() const {
         return D_.costNl == kCostLinear || D_.costL == kCostLinear || gNl() > 0 || gL() > 0 ||
-               D_.conNl == kConPolyhedronWithIdentity || D_.conL == kConPolyhedronWithIdentity;
+               D_.conNl == kConPolyhedronWithIdentity || D_.conL == kConPolyhedronWithIdentity ||
+               D_.conNl == kConRectangleInputBall;
     }
     size_t bLstar(bool dbl = false) const {
         const size_t in = (size_t)std::max(D_.ne * D_.dIV + idNl() + gNl() + D_.yD + 2 + 2 * D_.ne, D_.dVI + idL() + gL());
@@ -937,7 +925,7 @@ private:
         const size_t base = (size_t)std::max(D_.yD + 1 + idNl() + gNl() + D_.dIV, D_.dIV + idL() + gL() + D_.dVI);
         const size_t mats = 2 * lx() * D_.nx + lu() * D_.nu +
                             std::max((size_t)pad16(gNl()) * D_.nxu, (size_t)pad16(gL()) * D_.nx);
-        return (mats + ((size_t)std::max(D_.dIV, D_.dVI) + kTileWarps + (dbl ? 2 : 1) * (2 * in + base)) * kTileB) *
+        return (mats + ((size_t)std::max({D_.dIV, D_.dVI, D_.nu}) + kTileWarps + (dbl ? 2 : 1) * (2 * in + base)) * kTileB) *
                    sizeof(T) +
                (in + base) * sizeof(int);
     }
@@ -1010,11 +998,20 @@ private:
         part_ = dalloc<double>((size_t)chunks_ * nv_ * B_);
         const size_t Bi = (size_t)B_;
         int *ib = dalloc<int>(Bi * 16);
+        ib_ = ib;
         S_.phase = ib; S_.iOut = ib + Bi; S_.iIn = ib + 2 * Bi; S_.status = ib + 3 * Bi; S_.errInit = ib + 4 * Bi;
         S_.action = ib + 5 * Bi; S_.head = ib + 6 * Bi; S_.useAnd = ib + 7 * Bi; S_.iters = ib + 8 * Bi;
         S_.k0 = ib + 9 * Bi; S_.k1 = ib + 10 * Bi; S_.k2 = ib + 11 * Bi; S_.k2bt = ib + 12 * Bi; S_.k3 = ib + 13 * Bi;
         S_.calls = ib + 14 * Bi;
         double *db = dalloc<double>(Bi * (8 + 2 * kMaxAnderson * kMaxAnderson));
+        db_ = db;
+        if (B_ >= 2 * kTileB) {  // compaction workspaces
+            ibTmp_ = dalloc<int>(Bi * 16);
+            dbTmp_ = dalloc<double>(Bi * (8 + 2 * kMaxAnderson * kMaxAnderson));
+            from_ = dalloc<int>(Bi);
+        }
+        slotInst_.resize(Bi);
+        for (size_t q = 0; q < Bi; q++) slotInst_[q] = (int)q;
         S_.tau = db; S_.zeta = db + Bi; S_.w = db + 2 * Bi; S_.wSafe = db + 3 * Bi; S_.tol = db + 4 * Bi;
         S_.err = db + 5 * Bi; S_.coef = db + 6 * Bi; S_.G = db + 8 * Bi;
         S_.gamma = S_.G + Bi * kMaxAnderson * kMaxAnderson;
@@ -1149,8 +1146,9 @@ private:
 
     // Autotuner of the tile shapes of L, L* and the dynamics sweep: instance tiles per CTA in
     // {1, 2, 4, 8}, double-buffered when more than one and the shared memory allows.  Each
-    // candidate is timed over 3 launches of the T-form kernel (or 3 whole sweeps), with CUDA events
-    // on the solver stream; the fastest is kept.  Runs once, before the round is captured; it
+    // candidate is timed (best of two trials of 5 launches of the T-form kernel, or of 5 whole
+    // sweeps, with CUDA events on the solver stream); a larger shape replaces a smaller one only
+    // when it is at least 5% faster.  Runs once, before the round is captured; it
     // writes only CAND, R and the sweep's workspaces, which every round rewrites first.
     void autotune() {
         if (!batched_ || tuned_) return;
@@ -1160,15 +1158,19 @@ private:
         cudaEvent_t e0, e1;
         CK(cudaEventCreate(&e0));
         CK(cudaEventCreate(&e1));
-        auto timeIt = [&](auto launch) {
+        auto timeIt = [&](auto launch) {  // best of two trials of 5 launches after a warm-up
             launch();
-            CK(cudaEventRecord(e0, stream_));
-            for (int r = 0; r < 3; r++) launch();
-            CK(cudaEventRecord(e1, stream_));
-            CK(cudaEventSynchronize(e1));
-            float ms = 0;
-            CK(cudaEventElapsedTime(&ms, e0, e1));
-            return ms;
+            float best = 1e30f;
+            for (int trial = 0; trial < 2; trial++) {
+                CK(cudaEventRecord(e0, stream_));
+                for (int r = 0; r < 5; r++) launch();
+                CK(cudaEventRecord(e1, stream_));
+                CK(cudaEventSynchronize(e1));
+                float ms = 0;
+                CK(cudaEventElapsedTime(&ms, e0, e1));
+                best = std::min(best, ms);
+            }
+            return best;
         };
         float bestS = 1e30f, bestL = 1e30f;
         int tS = 1, tL = 1;
@@ -1177,9 +1179,9 @@ private:
             lstarDbl_ = tpc > 1 && canDblLstar();
             lopDbl_ = tpc > 1 && canDblLop();
             const float ms = timeIt([&] { launchLstar<0>(tevalLstarArgs()); });
-            if (ms < bestS) { bestS = ms; tS = tpc; }
+            if (ms < 0.95f * bestS) { bestS = ms; tS = tpc; }
             const float ml = timeIt([&] { launchLop<0>(tevalLopArgs()); });
-            if (ml < bestL) { bestL = ml; tL = tpc; }
+            if (ml < 0.95f * bestL) { bestL = ml; tL = tpc; }
         }
         tpcLstar_ = tS;
         lstarDbl_ = tS > 1 && canDblLstar();
@@ -1192,7 +1194,7 @@ private:
             backDbl_ = tpc > 1 && canDblBack();
             fwdDbl_ = tpc > 1 && canDblFwd();
             const float md = timeIt([&] { dynamics(); });
-            if (md < bestD) { bestD = md; tD = tpc; }
+            if (md < 0.95f * bestD) { bestD = md; tD = tpc; }
         }
         tpcDyn_ = tD;
         backDbl_ = tD > 1 && canDblBack();
@@ -1291,7 +1293,7 @@ private:
         A.maxOuter = opt_.maxOuter;
         A.maxInner = opt_.maxInner;
         A.ridge = sizeof(T) == 8 ? 1e-13 : 1e-7;
-        k_control<<<((int)B_ + 127) / 128, 128, 0, stream_>>>((int)B_, A);
+        k_control<<<((int)B_ + 3) / 4, 128, 0, stream_>>>((int)B_, A);  // 4 instances (warps) per block
         CK(cudaGetLastError());
     }
 
@@ -1300,14 +1302,6 @@ private:
         A.Z = Z_; A.CAND = CAND_; A.R = R_; A.PREV = PREV_; A.RPREV = RPREV_; A.BACKUP = BACKUP_; A.D = DIR_;
         A.ANDR = ANDR_; A.ANDZ = ANDZ_; A.action = S_.action; A.head = S_.head; A.useAnd = S_.useAnd;
         A.gamma = S_.gamma; A.tau = S_.tau; A.coef = S_.coef; A.m = (int)opt_.anderson;
-        if (B_ >= 32) {  // instance tiles x row chunks, about 8 blocks per SM
-            const long tiles = (B_ + 31) / 32;
-            const long chunks = std::max<long>(1, std::min<long>((152 * 8 + tiles - 1) / tiles, (D_.sZ + 7) / 8));
-            const long rows = (D_.sZ + chunks - 1) / chunks;
-            k_update_b<T><<<dim3((unsigned)tiles, (unsigned)((D_.sZ + rows - 1) / rows)), 256, 0, stream_>>>(D_, A, rows);
-            CK(cudaGetLastError());
-            return;
-        }
         const size_t total = (size_t)D_.sZ * B_;
         const int grid = (int)std::min<size_t>((total + 255) / 256, 152 * 8);
         k_update<T><<<grid, 256, 0, stream_>>>(D_, A);
@@ -1321,6 +1315,70 @@ private:
         controlLaunch(kSpock);
         updateLaunch();
         tileFlagsLaunch();
+    }
+
+    // Instance compaction.  The node kernels skip tiles of 32 instances that have all stopped, but
+    // a batch's slowest instances are spread over every tile.  When the running instances would
+    // fill at most 3/4 of the slots still in live tiles (and free two tiles or more), they are moved
+    // to the leading slots -- every buffer that carries state from round to round, the initial
+    // states and the controller state -- so only ceil(active / 32) tiles stay live.  The captured
+    // round reads the same buffers, which keep their addresses.  restoreOrder() puts every
+    // instance back in its own slot when the solve ends.
+    void maybeCompact(int active) {
+        if (!from_ || !batched_) return;
+        const long need = ((long)active + kTileB - 1) / kTileB * kTileB;
+        if (4 * (long)active > 3 * capacity_ || capacity_ - need < 2 * kTileB) return;
+        std::vector<int> st((size_t)B_);
+        CK(cudaMemcpyAsync(st.data(), S_.status, sizeof(int) * (size_t)B_, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+        std::vector<int> from;
+        from.reserve((size_t)B_);
+        for (long q = 0; q < B_; q++)
+            if (st[(size_t)q] == -1) from.push_back((int)q);
+        for (long q = 0; q < B_; q++)
+            if (st[(size_t)q] != -1) from.push_back((int)q);
+        permute(from);
+        capacity_ = need;
+        compactions_++;
+    }
+
+    void restoreOrder() {
+        bool ident = true;
+        for (long q = 0; q < B_; q++) ident = ident && slotInst_[(size_t)q] == (int)q;
+        if (ident) return;
+        std::vector<int> from((size_t)B_);
+        for (long q = 0; q < B_; q++) from[(size_t)slotInst_[(size_t)q]] = (int)q;  // instance q sits in slot ...
+        permute(from);
+    }
+
+    // Slot s takes the instance in slot from[s], in every persistent buffer.
+    void permute(const std::vector<int> &from) {
+        CK(cudaMemcpyAsync(from_, from.data(), sizeof(int) * (size_t)B_, cudaMemcpyHostToDevice, stream_));
+        auto gatherRows = [&](T *buf, long rows) {
+            const dim3 grid((unsigned)((B_ + 255) / 256), (unsigned)std::min<long>(rows, 8192));
+            k_gather_cols<T><<<grid, 256, 0, stream_>>>(W1_, buf, from_, rows, (int)B_);
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(buf, W1_, sizeof(T) * (size_t)rows * B_, cudaMemcpyDeviceToDevice, stream_));
+        };
+        const long nzr = D_.sZ;
+        for (T *buf : {Z_, PREV_, RPREV_, BACKUP_, DIR_}) gatherRows(buf, nzr);
+        for (long q = 0; q < opt_.anderson; q++) {
+            gatherRows(ANDR_ + (size_t)q * nzr * B_, nzr);
+            gatherRows(ANDZ_ + (size_t)q * nzr * B_, nzr);
+        }
+        gatherRows(x0s_, D_.nx);
+        const int perG = kMaxAnderson * kMaxAnderson, perGamma = kMaxAnderson;
+        k_gather_state<<<(int)((B_ + 255) / 256), 256, 0, stream_>>>(ibTmp_, ib_, dbTmp_, db_, from_, (int)B_, 16, 8, perG,
+                                                                    perGamma);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(ib_, ibTmp_, sizeof(int) * (size_t)B_ * 16, cudaMemcpyDeviceToDevice, stream_));
+        CK(cudaMemcpyAsync(db_, dbTmp_, sizeof(double) * (size_t)B_ * (8 + perG + perGamma), cudaMemcpyDeviceToDevice,
+                           stream_));
+        std::vector<int> inst((size_t)B_);
+        for (long q = 0; q < B_; q++) inst[(size_t)q] = slotInst_[(size_t)from[(size_t)q]];
+        slotInst_ = inst;
+        tileFlagsLaunch();
+        CK(cudaStreamSynchronize(stream_));
     }
 
     void ensureGraph() {

@@ -44,6 +44,7 @@ struct DevProblem {
     const T *NNtr, *b;
     const T *grad, *lGrad;  // linear costs: gradient per node ((nx + nu) x n) and of the leaves (nx)
     T step;
+    T radius;               // input ball of kConRectangleInputBall
 };
 
 // out = base + cL * Op(v), v = a1*in1 (+ a2*in2), base = b1*base1 (+ b2*base2).
@@ -110,6 +111,7 @@ public:
     // dynamics sweep's tiles per CTA (0: the small-batch kernels).  Runs the autotuner if needed.
     virtual void tuning(int *out5) = 0;
     long lastRounds() const { return lastRounds_; }
+    long lastCompactions() const { return lastCompactions_; }
     int device() const { return device_; }
     // Dynamics projection of a single-instance solver on caller-owned device memory: primUX is
     // the head [u | x] of a primal vector (solver precision), x0 the scaled initial state, and
@@ -123,7 +125,7 @@ public:
 protected:
     HostProblem hp_;
     long B_ = 1;
-    long lastRounds_ = 0, lastLaunches_ = 0;
+    long lastRounds_ = 0, lastLaunches_ = 0, lastCompactions_ = 0;
     int device_ = 0;
 };
 

@@ -178,7 +178,8 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem
     // constraint rows: identity part (rectangle, polyhedron with identity) and Gamma part
     // (polyhedron, polyhedron with identity); linear costs have 2-row IV / VI blocks [g'xu | t]
     const int con = nonleaf ? D.conNl : D.conL;
-    const int nId = (con == kConRectangle || con == kConPolyhedronWithIdentity) ? (nonleaf ? nxu : nx) : 0;
+    const int nId =
+        (con == kConRectangle || con == kConPolyhedronWithIdentity || con == kConRectangleInputBall) ? (nonleaf ? nxu : nx) : 0;
     const int nG = (con == kConPolyhedron || con == kConPolyhedronWithIdentity) ? (nonleaf ? D.gNl : D.gL) : 0;
     const bool linNl = D.costNl == kCostLinear, linL = D.costL == kCostLinear;
     // input row map
@@ -453,7 +454,8 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T
     // constraint rows of this node: an identity part (rectangle, polyhedron with identity) and a
     // Gamma part (polyhedron, polyhedron with identity); linear costs have a 2-row IV / VI
     const int con = nonleaf ? D.conNl : D.conL;
-    const int nId = (con == kConRectangle || con == kConPolyhedronWithIdentity) ? (nonleaf ? nxu : nx) : 0;
+    const int nId =
+        (con == kConRectangle || con == kConPolyhedronWithIdentity || con == kConRectangleInputBall) ? (nonleaf ? nxu : nx) : 0;
     const int nG = (con == kConPolyhedron || con == kConPolyhedronWithIdentity) ? (nonleaf ? D.gNl : D.gL) : 0;
     const bool linNl = D.costNl == kCostLinear, linL = D.costL == kCostLinear;
     const T g = P.step, gi = T(1) / P.step;
@@ -496,7 +498,7 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T
         return D.oVI + (long)l * dVI + (r - bVI);
     };
     const int inArr = A.in2 ? 2 : 1, baseArr = A.base2 ? 2 : (A.base1 ? 1 : 0);
-    const int dSoc = dIV > dVI ? dIV : dVI;
+    const int dSoc = max(max(dIV, dVI), nu);  // sw holds an SOC block or the inputs of an input ball
     const int ldx = pad16(nx), ldu = pad16(nu);
     const int matIV = linNl ? 0 : ldx * nx + ldu * nu, matVI = (!nonleaf && !linL) ? ldx * nx : 0;
     const int matG = nG ? pad16(nG) * (nonleaf ? nxu : nx) : 0;  // Gamma, padded column-major
@@ -617,7 +619,29 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T
                     FIN(rb, (v - boxProject(v, P.nlLo[bi], P.nlHi[bi])) * g);
                 } else EMIT(rb, lv);
             };
-            for (int k = warp; k < nId; k += kTileWarps) boxRow(bIII + k, k < nx ? INP(rx + k) : INP(ru + k - nx));
+            if (con == kConRectangleInputBall && MODE == 0) {
+                // box on the x rows; u * min(1, r / ||u||) on the u rows, the norm summed over warps
+                for (int k = warp; k < nx; k += kTileWarps) boxRow(bIII + k, INP(rx + k));
+                T ss = 0;
+                for (int k = warp; k < nu; k += kTileWarps) {
+                    const T v = (BASE(bIII + nx + k) + A.cL * INP(ru + k)) * gi;
+                    sw[k * kTileB + lane] = v;
+                    ss += v * v;
+                }
+                sPart[warp * kTileB + lane] = ss;
+                __syncthreads();
+                ss = 0;
+    #pragma unroll
+                for (int w = 0; w < kTileWarps; w++) ss += sPart[w * kTileB + lane];
+                const T nrm = sqrt(ss), f = nrm > P.radius ? P.radius / nrm : T(1);
+                for (int k = warp; k < nu; k += kTileWarps) {
+                    const T v = sw[k * kTileB + lane];
+                    FIN(bIII + nx + k, (v - f * v) * g);
+                }
+                __syncthreads();  // sw and sPart are reused below
+            } else {
+                for (int k = warp; k < nId; k += kTileWarps) boxRow(bIII + k, k < nx ? INP(rx + k) : INP(ru + k - nx));
+            }
             if (nG) {  // Gamma [x_j; u_j] (constraints.cuh:251-264, 386-401)
                 T accG[kMaxTasks][kRT];
                 zeroAcc(accG);
@@ -778,7 +802,7 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T
 // when `dbl` (the rows of tile t + 1 load while tile t is computed).
 // ------------------------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(kTileB *kTileWarps) k_dyn_back_b(const DevProblem<T> P, const Dims D, const PadMats<T> M,
+__global__ void __launch_bounds__(kTileB *kTileWarps, 2) k_dyn_back_b(const DevProblem<T> P, const Dims D, const PadMats<T> M,
                                                                   const T *__restrict__ cand, T *__restrict__ Q,
                                                                   T *__restrict__ DD, int stageFrom, int stage,
                                                                   int tilesPerCta, int dbl, const int *live) {
@@ -909,7 +933,7 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_dyn_back_b(const DevProb
 // candidate (x, u) and its residual Z - cand.  Tiles as in k_dyn_back_b.
 // ------------------------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(kTileB *kTileWarps) k_dyn_fwd_b(const DevProblem<T> P, const Dims D, const PadMats<T> M,
+__global__ void __launch_bounds__(kTileB *kTileWarps, 2) k_dyn_fwd_b(const DevProblem<T> P, const Dims D, const PadMats<T> M,
                                                                  T *__restrict__ cand, const T *__restrict__ DD,
                                                                  const T *__restrict__ x0s, int stageFrom,
                                                                  const T *__restrict__ Z, T *__restrict__ R,

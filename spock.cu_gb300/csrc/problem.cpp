@@ -157,11 +157,29 @@ int conKind(const std::string &s) {
     if (s == "rectangle") return kConRectangle;
     if (s == "polyhedron") return kConPolyhedron;
     if (s == "polyhedronWithIdentity") return kConPolyhedronWithIdentity;
-    fail("[parseConstraint] Constraint type " + s + " is not supported. Supported types include: none, rectangle, polyhedron, polyhedronWithIdentity");
+    if (s == "rectangleInputBall") return kConRectangleInputBall;
+    fail("[parseConstraint] Constraint type " + s + " is not supported. Supported types include: none, rectangle, polyhedron, polyhedronWithIdentity, rectangleInputBall");
 }
 
 // Bounds for one constraint part laid out like its dual block (constraints.cuh:32-37, 129-150,
 // 216-243, 316-360); the root's state bounds of a nonleaf rectangle are +-inf (constraints.cuh:142-148).
+// Rectangle bounds laid out like the dual block; the root's states are free (constraints.cuh:142-148).
+void loadConstraintRect(HostProblem &p, const std::string &dir, const std::string &part, long dpn, long nodes,
+                        std::vector<double> &lo, std::vector<double> &hi, long &per) {
+    const std::vector<double> ilb = expect(readTensor(dir, part + "ILB"), dpn, part + "ILB");
+    const std::vector<double> iub = expect(readTensor(dir, part + "IUB"), dpn, part + "IUB");
+    const double inf = std::numeric_limits<double>::infinity();
+    per = dpn;
+    lo.assign(per * nodes, 0.);
+    hi.assign(per * nodes, 0.);
+    for (long i = 0; i < nodes; i++)
+        for (long k = 0; k < dpn; k++) {
+            const bool freeRoot = i == 0 && k < p.nx;
+            lo[i * dpn + k] = freeRoot ? -inf : ilb[k];
+            hi[i * dpn + k] = freeRoot ? inf : iub[k];
+        }
+}
+
 void loadConstraint(HostProblem &p, const std::string &dir, bool leaf) {
     const std::string part = leaf ? "leafConstraint" : "nonleafConstraint";
     const int kind = leaf ? p.conLeaf : p.conNonleaf;
@@ -175,6 +193,13 @@ void loadConstraint(HostProblem &p, const std::string &dir, bool leaf) {
     std::vector<double> ilb, iub, glb, gub;
     gRows = 0;
     if (kind == kConNone) { per = 0; return; }
+    if (kind == kConRectangleInputBall) {
+        if (leaf) fail("[" + part + "] an input ball constrains nonleaf nodes only");
+        p.nlRadius = expect(readTensor(dir, part + "Radius"), 1, part + "Radius")[0];
+        if (!(p.nlRadius > 0)) fail("[" + part + "Radius] must be positive");
+        loadConstraintRect(p, dir, part, dpn, nodes, lo, hi, per);
+        return;
+    }
     if (kind == kConRectangle || kind == kConPolyhedronWithIdentity) {
         ilb = expect(readTensor(dir, part + "ILB"), dpn, part + "ILB");
         iub = expect(readTensor(dir, part + "IUB"), dpn, part + "IUB");

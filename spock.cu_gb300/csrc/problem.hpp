@@ -13,7 +13,15 @@
 namespace spock {
 
 enum CostKind { kCostQuadratic = 0, kCostLinear = 1, kCostQuadraticPlusLinear = 2 };
-enum ConstraintKind { kConNone = 0, kConRectangle = 1, kConPolyhedron = 2, kConPolyhedronWithIdentity = 3 };
+// kConRectangleInputBall (nonleaf only, no reference counterpart): box bounds on x and the ball
+// ||u||_2 <= nlRadius on the inputs; its dual block is [x; u] as for a rectangle.
+enum ConstraintKind {
+    kConNone = 0,
+    kConRectangle = 1,
+    kConPolyhedron = 2,
+    kConPolyhedronWithIdentity = 3,
+    kConRectangleInputBall = 4
+};
 
 struct HostProblem {
     std::string path;
@@ -37,6 +45,7 @@ struct HostProblem {
     // constraints: bounds laid out exactly like the dual block they bound
     std::vector<double> nlLower, nlUpper, lLower, lUpper, nlGamma, lGamma;
     long nlGammaRows = 0, lGammaRows = 0;
+    double nlRadius = 0.;  // kConRectangleInputBall
     // risk
     std::vector<double> NNtr, b;
     // iterate layout (cache.cuh:481-497, 529-581)

@@ -70,7 +70,7 @@ _SIGS = {
     "spock_apply_m": (ctypes.c_int, [_vp, _dp, _dp]),
     "spock_kernel_time": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int, _dp, _lp]),
     "spock_round_time": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
-    "spock_run_stats": (ctypes.c_int, [_vp, _lp, _lp]),
+    "spock_run_stats": (ctypes.c_int, [_vp, _lp, _lp, _lp]),
     "spock_tuning": (ctypes.c_int, [_vp, _ip]),
     "spock_counters_all": (ctypes.c_int, [_vp, _lp]),
     "spock_copy_iterate": (ctypes.c_int, [_vp, _vp]),
@@ -402,8 +402,14 @@ class Cache:
     def runStats(self):
         """(rounds, kernel launches) of the last solve."""
         r, l = ctypes.c_long(), ctypes.c_long()
-        _check(lib().spock_run_stats(self._h, ctypes.byref(r), ctypes.byref(l)))
+        _check(lib().spock_run_stats(self._h, ctypes.byref(r), ctypes.byref(l), None))
         return r.value, l.value
+
+    def compactions(self):
+        """Instance compactions of the last solve."""
+        c = ctypes.c_long()
+        _check(lib().spock_run_stats(self._h, None, None, ctypes.byref(c)))
+        return c.value
 
     def solveDevice(self, x0_device_ptr, algo=0):
         """Solve with initial states already on the device (nx x batch, element-major, in the

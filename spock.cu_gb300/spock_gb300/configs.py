@@ -12,7 +12,8 @@ Sizes:
            term (Factory.with_cost_scaling); the benchmark uses 1e-3, because at the literal
            scale (cost-to-go near 800) SPOCK stalls near a residual of 1e-2.
   config3: i.i.d. process with 5 equiprobable events, N=8, tau=3 -> 781 nodes; nx=100, nu=40;
-           dynamics generated as config2; quadratic costs; box on x; AVaR(0.9).
+           dynamics generated as config2; quadratic costs; box |x|<=3 and the input ball
+           ||u||_2 <= 2 (RectangleInputBall); AVaR(0.9).
 """
 import os
 
@@ -77,21 +78,22 @@ def config2(path, seed=0, count=1, nx=50, nu=20, horizon=10, stopping=4, states=
     return path, rng.uniform(-1., 1., size=(count, nx))
 
 
-def config3(path, seed=0, count=1):
+def config3(path, seed=0, count=1, nx=100, nu=40, horizon=8, stopping=3, events=5, radius=2.):
+    """Box |x| <= 3 on the states and the input ball ||u||_2 <= 2 (RectangleInputBall); the ball
+    needs equal input scales, so this problem is not preconditioned."""
     rng = np.random.default_rng(seed)
-    ne, nx, nu = 5, 100, 40
-    tree = F.IidProcess(np.ones(ne) / ne, horizon=8, stopping_stage=3).build()
-    dyn = _stable_dynamics(rng, nx, nu, ne)
+    tree = F.IidProcess(np.ones(events) / events, horizon=horizon, stopping_stage=stopping).build()
+    dyn = _stable_dynamics(rng, nx, nu, events)
     costs = [F.CostQuadratic(np.diag(rng.uniform(1., 10., nx)), np.diag(rng.uniform(.1, 1., nu)))
-             for _ in range(ne)]
+             for _ in range(events)]
     leaf = F.CostQuadratic(np.diag(rng.uniform(1., 10., nx)), leaf=True)
-    lb = np.concatenate((-3. * np.ones(nx), -2. * np.ones(nu)))
     (F.Factory(tree, nx, nu).with_dynamics_events(dyn)
      .with_cost_nonleaf_events(costs)
      .with_cost_leaf(leaf)
-     .with_constraint_nonleaf(F.Rectangle(lb, -lb))
+     .with_constraint_nonleaf(F.RectangleInputBall(-3. * np.ones(nx), 3. * np.ones(nx), nu, radius))
      .with_constraint_leaf(F.Rectangle(-3. * np.ones(nx), 3. * np.ones(nx)))
      .with_risk(F.AVaR(.9))
+     .with_preconditioning(False)
      .generate_problem(path))
     return path, rng.uniform(-1., 1., size=(count, nx))
 

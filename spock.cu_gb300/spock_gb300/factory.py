@@ -210,6 +210,23 @@ class Rectangle:
             raise ValueError("Rectangle constraint bounds invalid")
 
 
+class RectangleInputBall:
+    """Nonleaf constraint (not in the reference): box bounds on the states and the Euclidean ball
+    ||u||_2 <= radius on the inputs -- the second-order-cone input constraint ||u||_2 <= r with a
+    fixed r.  Its dual block is [x; u] as for a rectangle; the projection clamps the x rows and
+    scales u by min(1, r / ||u||)."""
+    kind = "rectangleInputBall"
+
+    def __init__(self, x_lb, x_ub, num_inputs, radius):
+        x_lb, x_ub = np.asarray(x_lb, float).ravel(), np.asarray(x_ub, float).ravel()
+        if x_lb.size != x_ub.size or (x_lb > x_ub).any() or not radius > 0:
+            raise ValueError("RectangleInputBall constraint invalid")
+        self.lb = np.concatenate((x_lb, -np.inf * np.ones(num_inputs)))
+        self.ub = np.concatenate((x_ub, np.inf * np.ones(num_inputs)))
+        self.nx = x_lb.size
+        self.radius = float(radius)
+
+
 class Polyhedron:
     kind = "polyhedron"
 
@@ -463,6 +480,12 @@ class Problem:
             return None
         if con.kind == "rectangle":
             return (con.lb * scale, con.ub * scale)
+        if con.kind == "rectangleInputBall":
+            su = scale[con.nx:]
+            if not np.allclose(su, su[0]):
+                raise ValueError("an input ball needs the same preconditioning scale on every input "
+                                 "(or with_preconditioning(False))")
+            return (con.lb * scale, con.ub * scale, con.radius * su[0])
         if con.kind == "polyhedron":
             return (con.G / scale[None, :], con.lb, con.ub)
         raise ValueError("constraint kind %s not supported by this factory" % con.kind)
@@ -496,7 +519,7 @@ class Problem:
         t, nx, nu = self.tree, self.nx, self.nu
         n, nnl, nl = t.num_nodes, t.num_nonleaf_nodes, t.num_leaf_nodes
         self.size_prim = (nu + self.y_dim) * nnl + (nx + 2) * n
-        d3 = {"no": 0, "rectangle": nx + nu}.get(self.nl_con.kind, None)
+        d3 = {"no": 0, "rectangle": nx + nu, "rectangleInputBall": nx + nu}.get(self.nl_con.kind, None)
         d3 = self.nl_bounds[0].shape[0] if d3 is None else d3
         d5 = {"no": 0, "rectangle": nx}.get(self.l_con.kind, None)
         d5 = self.l_bounds[0].shape[0] if d5 is None else d5
@@ -522,7 +545,7 @@ class Problem:
         u, x, y, tt, s = self._split_prim(p)
         out = [y.ravel(), s[:nnl] - np.einsum("ij,ij->i", self.b, y)]
         xu = np.concatenate((x[:nnl], u), axis=1)
-        if self.nl_con.kind == "rectangle":
+        if self.nl_con.kind in ("rectangle", "rectangleInputBall"):
             out.append(xu.ravel())
         elif self.nl_con.kind == "polyhedron":
             out.append((xu @ self.nl_bounds[0].T).ravel())
@@ -570,7 +593,7 @@ class Problem:
         s = np.zeros(n)
         s[:nnl] = II
         y = I - self.b * II[:, None]
-        if self.nl_con.kind == "rectangle":
+        if self.nl_con.kind in ("rectangle", "rectangleInputBall"):
             III = d[o:o + (nx + nu) * nnl].reshape(nnl, nx + nu); o += (nx + nu) * nnl
             x[:nnl] = III[:, :nx]
             u[:] = III[:, nx:]
@@ -662,9 +685,11 @@ class Problem:
                 w("leafCost_q", self.lq)
         for txt, con, bnd in (("nonleafConstraint", self.nl_con, self.nl_bounds),
                               ("leafConstraint", self.l_con, self.l_bounds)):
-            if con.kind == "rectangle":
+            if con.kind in ("rectangle", "rectangleInputBall"):
                 w(txt + "ILB", bnd[0])
                 w(txt + "IUB", bnd[1])
+                if con.kind == "rectangleInputBall":
+                    w(txt + "Radius", np.array([bnd[2]]))
             elif con.kind == "polyhedron":
                 w(txt + "Gamma", bnd[0])
                 w(txt + "GLB", bnd[1])

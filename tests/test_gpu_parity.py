@@ -258,42 +258,39 @@ def test_full_size_dynamics_feasible(oracle_lib, tmp_problems, batch):
 
 
 def test_resolve_from_previous_solution(oracle_lib):
-    """spock_resolve: 64 cfg1 instances re-solved warm from their previous solutions after a small
-    move of x0 (the previousSolution path, cache.cuh:611-632, kept on the device) converge, and
-    their first inputs agree with cold solves of the same states."""
-    path = os.path.join(GOLDEN, "cfg1")
+    """spock_resolve: 32 instances of the reference's test problem re-solved warm from their
+    previous solutions after a small move of x0 (the previousSolution path, cache.cuh:611-632,
+    kept on the device) converge, and their first inputs agree with cold solves of the same
+    states."""
+    path = os.path.join(GOLDEN, "reftest")
     P = oracle_lib.Problem(path)
-    rng = np.random.default_rng(21)
-    x0s = rng.uniform(-1, 1, (64, P.nx))
-    # a warm start captures a small initial error, so the absolute tolerance decides: FP64 and a
-    # generous cap keep the slowest instances inside it
-    t, d, c = make(path, 64, batch=64, tol=1e-3, max_iters=20000)
+    x0s = np.full((32, P.nx), 1.1) + np.linspace(-.05, .05, 32)[:, None]
+    t, d, c = make(path, 64, batch=32, tol=1e-8, max_iters=20000)
     assert (c.runSpockBatch(x0s) == 0).all()
-    x1 = x0s + rng.uniform(-.05, .05, x0s.shape)
+    x1 = x0s + np.random.default_rng(21).uniform(-.01, .01, x0s.shape)
     assert (c.resolveBatch(x1) == 0).all()
     u_warm = c.firstInputs()
-    t2, d2, c2 = make(path, 64, batch=64, tol=1e-3, max_iters=20000)
+    t2, d2, c2 = make(path, 64, batch=32, tol=1e-8, max_iters=20000)
     assert (c2.runSpockBatch(x1) == 0).all()
-    assert np.abs(u_warm - c2.firstInputs()).max() <= 2e-2 * max(1., np.abs(c2.firstInputs()).max())
+    assert np.abs(u_warm - c2.firstInputs()).max() <= 1e-5 * max(1., np.abs(c2.firstInputs()).max())
 
 
 def test_converged_instances_stay_put(oracle_lib):
     """Per-instance convergence masks: in a batch whose instances stop at very different
-    iterations (half of them start at their own solution), the early ones keep the solution they
-    stopped at while the node kernels skip their tiles."""
-    path = os.path.join(GOLDEN, "cfg1")
+    iterations (the first tile starts at its own solution, the second cold), the early ones keep
+    the solution they stopped at while the node kernels skip their tile."""
+    path = os.path.join(GOLDEN, "reftest")
     P = oracle_lib.Problem(path)
-    rng = np.random.default_rng(22)
-    x0s = rng.uniform(-1, 1, (64, P.nx))
-    t, d, c = make(path, 64, batch=64, tol=1e-6, max_iters=5000)
+    x0s = np.full((64, P.nx), 1.1) + np.linspace(-.05, .05, 64)[:, None]
+    t, d, c = make(path, 64, batch=64, tol=1e-8, max_iters=20000)
     assert (c.runSpockBatch(x0s) == 0).all()
     z = c.solutions()
     warm = z.copy()
-    warm[32:] = 0.  # tiles 0 (warm, stop early) and 1 (cold, run long)
+    warm[32:] = 0.
     assert (c.runSpockBatch(x0s, prev=warm) == 0).all()
     it = c.solveIters()
     assert it[:32].max() < it[32:].min()
-    assert np.abs(c.solutions()[:32] - z[:32]).max() <= 1e-5 * max(1., np.abs(z).max())
+    assert np.abs(c.solutions()[:32] - z[:32]).max() <= 1e-6 * max(1., np.abs(z).max())
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -323,3 +320,53 @@ def test_fp64_polish_of_fp32_solve(oracle_lib):
         z, s = P.run(x0s[b], oracle_lib.options(tol=1e-9, max_iters=20000), "spock")
         u_ref = P.states_inputs(z)[1][:P.nu]
         assert np.abs(u0[b] - u_ref).max() <= 1e-6 * max(1., np.abs(u_ref).max()), b
+
+
+@pytest.mark.parametrize("batch", [1, 32])
+def test_input_ball_constraint(oracle_lib, tmp_problems, batch):
+    """The input-ball constraint ||u||_2 <= r of config 3 on a small problem: the T step matches
+    the oracle (FP64 1e-10, FP32 1e-4), and an FP64 SPOCK solve converges with the oracle's u_0
+    and keeps every input inside the ball."""
+    from spock_gb300 import configs
+    path, x0 = configs.cached("config3", tmp_problems, seed=1, count=1, nx=4, nu=3, horizon=3, stopping=2,
+                              events=2, radius=.5)
+    P = oracle_lib.Problem(path)
+    rng = np.random.default_rng(41)
+    for prec, tol in [(64, 1e-10), (32, 1e-4)]:
+        t, d, c = make(path, prec, batch=batch)
+        for _ in range(3):
+            z = 3 * rng.standard_normal(P.size)
+            assert rel(c.cpStep(x0[0], z), P.cp_step(x0[0], z)) < tol
+    t, d, c = make(path, 64, batch=batch, tol=1e-8, max_iters=20000)
+    assert c.runSpock(x0[0]) == 0
+    z, s = P.run(x0[0], oracle_lib.options(tol=1e-8, max_iters=20000), "spock")
+    assert s.status == 0
+    u_ref = P.states_inputs(z)[1]
+    u = c.inputs()
+    assert np.abs(u[:P.nu] - u_ref[:P.nu]).max() <= 1e-5 * max(1., np.abs(u_ref).max())
+    assert np.linalg.norm(u.reshape(-1, P.nu), axis=1).max() <= .5 * (1 + 1e-4)
+
+
+def test_instance_compaction(oracle_lib):
+    """Instance compaction: in a batch of 128 where every fourth instance starts cold and the others
+    at their solution, the cold ones -- spread over all four tiles -- are moved to the leading slots
+    once the warm ones stop.  Every instance still converges to its own solution (u_0 against the
+    oracle), and the warm ones keep theirs."""
+    path = os.path.join(GOLDEN, "reftest")
+    P = oracle_lib.Problem(path)
+    x0s = np.full((128, P.nx), 1.1) + np.linspace(-.05, .05, 128)[:, None]
+    t, d, c = make(path, 64, batch=128, tol=1e-8, max_iters=20000)
+    assert (c.runSpockBatch(x0s) == 0).all()
+    z = c.solutions()
+    warm = z.copy()
+    warm[::4] = 0.
+    assert (c.runSpockBatch(x0s, prev=warm) == 0).all()
+    assert c.compactions() >= 1
+    u0 = c.firstInputs()
+    for b in (0, 4, 124):
+        zr, s = P.run(x0s[b], oracle_lib.options(tol=1e-8, max_iters=20000), "spock")
+        u_ref = P.states_inputs(zr)[1][:P.nu]
+        assert np.abs(u0[b] - u_ref).max() <= 1e-6 * max(1., np.abs(u_ref).max()), b
+    keep = np.ones(128, bool)
+    keep[::4] = False
+    assert np.abs(c.solutions()[keep] - z[keep]).max() <= 1e-6 * max(1., np.abs(z).max())

@@ -165,3 +165,27 @@ def test_spock_and_cp_agree(oracle_lib):
     assert np.allclose(u1[:P.nu], u2[:P.nu], atol=1e-7)
     s0 = P.size_prim - P.n
     assert abs(z1[s0] - z2[s0]) <= 1e-6 * abs(z2[s0])
+
+
+def test_input_ball_projection(oracle_lib, tmp_problems):
+    """RectangleInputBall (the second-order-cone input constraint ||u||_2 <= r): after the dual
+    projection every nonleaf node's u rows lie in the ball, rows inside it are unchanged, and the
+    x rows are clamped to their box (the root's states are free)."""
+    from spock_gb300 import configs
+    path, _ = configs.cached("config3", tmp_problems, seed=1, count=1, nx=4, nu=3, horizon=3, stopping=2,
+                             events=2, radius=.5)
+    P = oracle_lib.Problem(path)
+    rng = np.random.default_rng(3)
+    d = 2 * rng.standard_normal(P.size_dual)
+    out = P.project_dual(d)
+    nxu = P.nx + P.nu
+    oIII = P.ydim * P.nnl + P.nnl
+    for i in range(P.nnl):
+        u0 = d[oIII + i * nxu + P.nx:oIII + (i + 1) * nxu]
+        u1 = out[oIII + i * nxu + P.nx:oIII + (i + 1) * nxu]
+        n0 = np.linalg.norm(u0)
+        assert np.linalg.norm(u1) <= .5 + 1e-12
+        assert np.allclose(u1, u0 if n0 <= .5 else u0 * .5 / n0, atol=1e-14)
+        x1 = out[oIII + i * nxu:oIII + i * nxu + P.nx]
+        if i > 0:
+            assert (np.abs(x1) <= 3 + 1e-12).all()
