@@ -102,6 +102,10 @@ int spock_resolve_device(spock_solver s, int algo, const void *x0_device, int *s
  * following spock_resolve(dst, ...) with the same initial states is the FP64 polish of the FP32
  * solution (it continues from it under dst's tolerances).  No reference counterpart. */
 int spock_copy_iterate(spock_solver dst, spock_solver src);
+/* Replace the solver's iterate by a device array of sizePrimal + sizeDual rows x batch columns,
+ * element-major (z[k * batch + b]), FP32 (bits = 32) or FP64 (64), converted on the device; a
+ * following spock_resolve starts every instance from it (a warm start predicted on the GPU). */
+int spock_set_iterate_device(spock_solver s, const void *z_device, int bits);
 
 /* Results.  Cache::solution() (cache.cuh:378): the raw iterate of one instance, sizePrimal +
  * sizeDual doubles.  Cache::states()/inputs() (cache.cuh:386-412): unscaled, nx*numNodes and
@@ -140,6 +144,10 @@ int spock_run_stats(spock_solver s, long *rounds, long *launches, long *compacti
  * double-buffered, dynamics-sweep tiles per CTA (0 when the small-batch kernels run)}.  No
  * reference counterpart. */
 int spock_tuning(spock_solver s, int *out5);
+/* Override the autotuner: in3 = {L* tiles per CTA, L tiles per CTA, dynamics-sweep tiles per CTA},
+ * each 1, 2, 4 or 8 (double-buffered where two tiles fit in shared memory).  No effect on the
+ * small-batch kernels.  No reference counterpart. */
+int spock_set_tuning(spock_solver s, const int *in3);
 
 /* Dynamics projection that allocates no device memory.  No counterpart in the reference: it
  * is for callers that cannot allocate while they solve, such as a control loop re-solving
@@ -156,6 +164,23 @@ int spock_tuning(spock_solver s, int *out5);
  * make that first call before any stream capture.  All calls share the one buffer: calls that
  * overlap on the GPU (other threads, other streams) race with each other. */
 int spock_project_dynamics_noalloc(spock_solver s, const void *x0, void *prim_ux, void *stream);
+
+/* ---- Learned warm start (no reference counterpart).  A three-layer MLP x0 -> coefficients of a
+ * solution basis, trained and evaluated by the library's own kernels: dims4 = {inputs, hidden,
+ * hidden, outputs}; GELU (tanh form) after the two hidden layers; BF16 weight copies read by every
+ * product, FP32 master weights updated by Adam, FP32 accumulation.  Tensors are column-major
+ * float device arrays with one sample per column.  Parameters pack W1 (d1 x d0), b1, W2 (d2 x d1),
+ * b2, W3 (d3 x d2), b3. */
+typedef struct spock_mlp_s *spock_mlp;
+int spock_mlp_create(const int *dims4, int device, spock_mlp *out);
+void spock_mlp_free(spock_mlp m);
+long spock_mlp_param_count(spock_mlp m);
+int spock_mlp_set_params(spock_mlp m, const float *params);              /* host -> master + BF16 */
+int spock_mlp_get_params(spock_mlp m, float *params, float *grads);       /* host copies; NULL skips */
+int spock_mlp_forward(spock_mlp m, const void *x_device, int cols, void *y_device);
+/* forward, mean-squared-error gradient against t_device (d3 x cols), and an Adam step (lr > 0;
+ * lr = 0 only computes the gradients); *loss = mean squared error before the step. */
+int spock_mlp_train_step(spock_mlp m, const void *x_device, const void *t_device, int cols, float lr, float *loss);
 
 #ifdef __cplusplus
 }

@@ -14,7 +14,7 @@ SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libspock_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["engine.cu", "problem.cpp", "capi.cpp", "noalloc.cu", "offline.cu"]
+SOURCES = ["engine.cu", "problem.cpp", "capi.cpp", "noalloc.cu", "offline.cu", "mlp.cu"]
 
 
 def nvcc():

@@ -216,6 +216,16 @@ int spock_resolve_device(spock_solver sv, int algo, const void *x0, int *statuse
     });
 }
 
+int spock_set_iterate_device(spock_solver sv, const void *z_device, int bits) {
+    return guard([&] {
+        auto *s = solver(sv);
+        need(z_device, "z");
+        if (bits != 32 && bits != 64) throw std::invalid_argument("[setIterate] bits must be 32 or 64");
+        s->eng->setIterateFromDevice(z_device, bits, s->eng->problem().sizeIterate(), s->eng->batch(),
+                                     s->eng->device());
+    });
+}
+
 int spock_copy_iterate(spock_solver dst, spock_solver src) {
     return guard([&] {
         auto *d = solver(dst);
@@ -367,6 +377,13 @@ int spock_tuning(spock_solver sv, int *out5) {
     return guard([&] {
         if (!out5) throw std::invalid_argument("[spock_tuning] null output");
         solver(sv)->eng->tuning(out5);
+    });
+}
+
+int spock_set_tuning(spock_solver sv, const int *in3) {
+    return guard([&] {
+        need(in3, "tiles");
+        solver(sv)->eng->setTuning(in3[0], in3[1], in3[2]);
     });
 }
 

@@ -303,6 +303,75 @@ struct UpdArgs {
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_update(const Dims Dm, const UpdArgs<T> A) {
+    // thread = instance b (x) and a stride of rows (y): consecutive lanes touch consecutive
+    // instances of a row (coalesced), the action is read once, and the row loop is unrolled over
+    // non-aliasing pointers so several rows' loads are in flight per thread
+    const int B = Dm.B;
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    const size_t slot = (size_t)Dm.sZ * B;
+    const int act = A.action[b];
+    if (act == kActNone || act == kActBK1) return;
+    T *__restrict__ Z = A.Z;
+    const T *__restrict__ CAND = A.CAND;
+    const T *__restrict__ R = A.R;
+    const long step = gridDim.y, k0 = blockIdx.y, n = Dm.sZ;
+    if (act == kActAK0 || act == kActALs) {
+        T *__restrict__ PREV = A.PREV;
+        T *__restrict__ RPREV = A.RPREV;
+        T *__restrict__ BACKUP = A.BACKUP;
+        T *__restrict__ D = A.D;
+        T *__restrict__ ANDR = A.ANDR;
+        T *__restrict__ ANDZ = A.ANDZ;
+        const int m = A.m;
+        const int h = (A.head[b] + m - 1) % m;  // slot written this round (head already advanced)
+        T g[kMaxAnderson];
+        const bool useAnd = A.useAnd[b];
+#pragma unroll
+        for (int s2 = 0; s2 < kMaxAnderson; s2++)
+            g[s2] = (useAnd && s2 < m && s2 != h) ? T(A.gamma[(size_t)b * kMaxAnderson + s2]) : T(0);
+        const T gh = useAnd ? T(A.gamma[(size_t)b * kMaxAnderson + h]) : T(0);
+#pragma unroll 4
+        for (long k = k0; k < n; k += step) {
+            const size_t o = (size_t)k * B + b;
+            const T z = Z[o], r = R[o], c = CAND[o];
+            const T dr = r - RPREV[o];
+            const T dzr = (z - PREV[o]) - dr;
+            T d = -r - gh * dzr;
+#pragma unroll
+            for (int s2 = 0; s2 < kMaxAnderson; s2++)
+                if (s2 < m && s2 != h) d -= g[s2] * ANDZ[s2 * slot + o];
+            ANDR[h * slot + o] = dr;
+            ANDZ[h * slot + o] = dzr;
+            D[o] = d;
+            PREV[o] = z;
+            RPREV[o] = r;
+            BACKUP[o] = c;
+            Z[o] = z + d;
+        }
+        return;
+    }
+    const T cf = act == kActBK2 ? T(A.coef[b]) : T(0), tau = act == kActBBt ? T(A.tau[b]) : T(0);
+    const T *__restrict__ PREVc = A.PREV;
+    const T *__restrict__ BACKUPc = A.BACKUP;
+    const T *__restrict__ Dc = A.D;
+#pragma unroll 4
+    for (long k = k0; k < n; k += step) {
+        const size_t o = (size_t)k * B + b;
+        switch (act) {
+            case kActFinish:
+            case kActCp: Z[o] = CAND[o]; break;
+            case kActBK2: Z[o] = PREVc[o] - cf * R[o]; break;
+            case kActBK3: Z[o] = BACKUPc[o]; break;
+            case kActBBt: Z[o] = PREVc[o] + tau * Dc[o]; break;
+            default: break;
+        }
+    }
+}
+
+// Batches below one tile: one thread per element (consecutive elements, consecutive threads).
+template <typename T>
+__global__ void __launch_bounds__(256) k_update_flat(const Dims Dm, const UpdArgs<T> A) {
     const int B = Dm.B;
     const size_t total = (size_t)Dm.sZ * B;
     const size_t slot = (size_t)Dm.sZ * B;
@@ -669,6 +738,24 @@ public:
         uploadSlice(R_, z, 0, D_.sZ);
         applyMres();
         downloadSlice(MR_, mz, 0, D_.sZ);
+    }
+
+    void setTuning(int lstar, int lop, int dyn) override {
+        for (int v : {lstar, lop, dyn})
+            if (v != 1 && v != 2 && v != 4 && v != 8) throw std::invalid_argument("[tuning] tiles per CTA must be 1, 2, 4 or 8");
+        if (!batched_) return;
+        tuned_ = true;
+        tpcLstar_ = lstar;
+        lstarDbl_ = lstar > 1 && canDblLstar();
+        tpcLop_ = lop;
+        lopDbl_ = lop > 1 && canDblLop();
+        tpcDyn_ = dyn;
+        backDbl_ = dyn > 1 && canDblBack();
+        fwdDbl_ = dyn > 1 && canDblFwd();
+        if (graph_) {  // the captured round has the old launch shapes
+            CK(cudaGraphExecDestroy(graph_));
+            graph_ = nullptr;
+        }
     }
 
     void tuning(int *out5) override {
@@ -1302,9 +1389,16 @@ private:
         A.Z = Z_; A.CAND = CAND_; A.R = R_; A.PREV = PREV_; A.RPREV = RPREV_; A.BACKUP = BACKUP_; A.D = DIR_;
         A.ANDR = ANDR_; A.ANDZ = ANDZ_; A.action = S_.action; A.head = S_.head; A.useAnd = S_.useAnd;
         A.gamma = S_.gamma; A.tau = S_.tau; A.coef = S_.coef; A.m = (int)opt_.anderson;
-        const size_t total = (size_t)D_.sZ * B_;
-        const int grid = (int)std::min<size_t>((total + 255) / 256, 152 * 8);
-        k_update<T><<<grid, 256, 0, stream_>>>(D_, A);
+        if (B_ < 32) {
+            const size_t total = (size_t)D_.sZ * B_;
+            const int grid = (int)std::min<size_t>((total + 255) / 256, 152 * 8);
+            k_update_flat<T><<<grid, 256, 0, stream_>>>(D_, A);
+            CK(cudaGetLastError());
+            return;
+        }
+        const long bx = (B_ + 255) / 256;  // about 8 blocks of 256 threads per SM
+        const long by = std::max<long>(1, std::min<long>((152 * 8 + bx - 1) / bx, D_.sZ));
+        k_update<T><<<dim3((unsigned)bx, (unsigned)by), 256, 0, stream_>>>(D_, A);
         CK(cudaGetLastError());
     }
 

@@ -110,6 +110,9 @@ public:
     // Tile shapes in use: L* instance tiles per CTA, L* double-buffered, the same for L, and the
     // dynamics sweep's tiles per CTA (0: the small-batch kernels).  Runs the autotuner if needed.
     virtual void tuning(int *out5) = 0;
+    // Override the tuner: tiles per CTA of L*, L and the dynamics sweep (1, 2, 4 or 8), double
+    // buffering where more than one tile fits twice in shared memory.
+    virtual void setTuning(int lstar, int lop, int dyn) = 0;
     long lastRounds() const { return lastRounds_; }
     long lastCompactions() const { return lastCompactions_; }
     int device() const { return device_; }

@@ -25,6 +25,11 @@ constexpr int kMaxTasks = 2;   // register blocks per warp: rows <= 16 * 8 * 2 =
 
 __host__ __device__ inline int pad16(int r) { return (r + 15) & ~15; }
 
+// L and L* keep two CTAs on an SM in FP32 (their shared memory allows it, so registers are capped
+// at 128); in FP64 the shared memory of one CTA already fills the SM.
+template <typename T>
+constexpr int kOpCtasPerSm = sizeof(T) == 4 ? 2 : 1;
+
 // Register blocks of a matrix with `rows` rows, and the slot a warp takes in a matrix whose
 // blocks are dealt out starting at warp `first` (so two matrices accumulated side by side,
 // e.g. sqrt(Q) and sqrt(R), keep different warps busy).
@@ -165,7 +170,7 @@ __device__ __forceinline__ void gather(T *sm, int n, const T *src, int B, int b0
 // base rows,  nonleaf i: [x_i][u_i][y_i][t_ch][s_ch][t_0 s_0 at the root];  leaf: [x_i]
 // ------------------------------------------------------------------------------------------
 template <typename T, int MODE>
-__global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem<T> P, const Dims D, const OpArgs<T> A,
+__global__ void __launch_bounds__(kTileB *kTileWarps, kOpCtasPerSm<T>) k_lstar_b(const DevProblem<T> P, const Dims D, const OpArgs<T> A,
                                                                 const PadMats<T> M, int tilesPerCta, int dbl) {
     extern __shared__ __align__(16) unsigned char smraw[];
     T *sm = reinterpret_cast<T *>(smraw);
@@ -441,7 +446,7 @@ __global__ void __launch_bounds__(kTileB *kTileWarps) k_lstar_b(const DevProblem
 // base rows:  nonleaf j: [I_j][II_j][III_j][IV_j];  leaf j: [IV_j][V_l][VI_l]
 // ------------------------------------------------------------------------------------------
 template <typename T, int MODE>
-__global__ void __launch_bounds__(kTileB *kTileWarps) k_lop_b(const DevProblem<T> P, const Dims D, const OpArgs<T> A,
+__global__ void __launch_bounds__(kTileB *kTileWarps, kOpCtasPerSm<T>) k_lop_b(const DevProblem<T> P, const Dims D, const OpArgs<T> A,
                                                               const PadMats<T> M, int tilesPerCta, int dbl) {
     extern __shared__ __align__(16) unsigned char smraw[];
     T *sm = reinterpret_cast<T *>(smraw);

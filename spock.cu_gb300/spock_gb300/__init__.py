@@ -73,7 +73,16 @@ _SIGS = {
     "spock_run_stats": (ctypes.c_int, [_vp, _lp, _lp, _lp]),
     "spock_tuning": (ctypes.c_int, [_vp, _ip]),
     "spock_counters_all": (ctypes.c_int, [_vp, _lp]),
+    "spock_set_tuning": (ctypes.c_int, [_vp, _ip]),
     "spock_copy_iterate": (ctypes.c_int, [_vp, _vp]),
+    "spock_set_iterate_device": (ctypes.c_int, [_vp, _vp, ctypes.c_int]),
+    "spock_mlp_create": (ctypes.c_int, [_ip, ctypes.c_int, ctypes.POINTER(_vp)]),
+    "spock_mlp_free": (None, [_vp]),
+    "spock_mlp_param_count": (ctypes.c_long, [_vp]),
+    "spock_mlp_set_params": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_float)]),
+    "spock_mlp_get_params": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
+    "spock_mlp_forward": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _vp]),
+    "spock_mlp_train_step": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_float, ctypes.POINTER(ctypes.c_float)]),
     "spock_offline_dynamics": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp, _dp]),
     "spock_resolve": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.c_long, _ip, _lp]),
     "spock_resolve_device": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _ip, _lp]),
@@ -292,6 +301,10 @@ class Cache:
                                           self._status.ctypes.data_as(_ip), self._iters.ctypes.data_as(_lp)))
         return self._status.copy()
 
+    def setIterateDevice(self, z_device_ptr, bits):
+        """Take the iterate from a device array (sizeIterate x batch, element-major, FP32 or FP64)."""
+        _check(lib().spock_set_iterate_device(self._h, ctypes.c_void_p(z_device_ptr), int(bits)))
+
     def copyIterateFrom(self, other):
         """Take another solver's current iterate (same problem and batch, same GPU), converted to
         this solver's precision on the device."""
@@ -398,6 +411,11 @@ class Cache:
         _check(lib().spock_tuning(self._h, out.ctypes.data_as(_ip)))
         return dict(zip(["lstar_tiles_per_cta", "lstar_double_buffer", "lop_tiles_per_cta", "lop_double_buffer",
                          "dyn_tiles_per_cta"], out.tolist()))
+
+    def setTuning(self, lstar, lop, dyn):
+        """Override the autotuner's tiles per CTA (1, 2, 4 or 8) for L*, L and the dynamics sweep."""
+        v = np.array([lstar, lop, dyn], dtype=np.int32)
+        _check(lib().spock_set_tuning(self._h, v.ctypes.data_as(_ip)))
 
     def runStats(self):
         """(rounds, kernel launches) of the last solve."""
