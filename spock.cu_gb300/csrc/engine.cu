@@ -1004,7 +1004,7 @@ private:
         const size_t base = (size_t)std::max(D_.nxu + D_.yD + 2 * D_.ne + 2, D_.nx);
         const size_t mats = std::max((size_t)D_.ne * (lx() * D_.nx + lu() * D_.nu + lx() + lu()), lx() * D_.nx + lx()) +
                             std::max((size_t)pad16(D_.nxu) * gNl(), (size_t)pad16(D_.nx) * gL());
-        const size_t gv = (gNl() || gL()) ? (size_t)D_.nxu : 0;
+        const size_t gv = (gNl() || gL() || D_.costNl == kCostLinear || D_.costL == kCostLinear) ? (size_t)D_.nxu : 0;
         return (mats + ((dbl ? 2 : 1) * (in + base) + (size_t)D_.nd + gv) * kTileB) * sizeof(T) + (in + base) * sizeof(int);
     }
     size_t bLop(bool dbl = false) const {

@@ -231,7 +231,9 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, kOpCtasPerSm<T>) k_lstar_b
     const int bufElems = (nIn * inArr + nBase * baseArr) * kTileB;  // one tile's input and base rows
     T *sMat = sm, *sGT = sMat + matElems - matG, *sBuf = sMat + matElems;
     T *sAv = sBuf + (dbl ? 2 : 1) * bufElems;  // the 4E+1 vector of the kernel projection
-    T *sGv = sAv + D.nd * kTileB;              // Gamma' times the constraint rows, dG x 32
+    // per-row extra terms of x_i / u_i (Gamma' times the Gamma rows, linear-cost gradients), dG x 32
+    const bool extra = nG > 0 || (nonleaf ? linNl : linL);
+    T *sGv = sAv + D.nd * kTileB;
     if (nG) stageMat(sGT, nonleaf ? M.nlGT : M.lGT, matG);
     if (nonleaf && !linNl) {
         const bool qplNl = D.costNl == kCostQuadraticPlusLinear;
@@ -261,7 +263,7 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, kOpCtasPerSm<T>) k_lstar_b
     }
     // The node's row maps, evaluated once per CTA into shared memory: every tile's gathers and
     // output writes then take their iterate rows from these tables.
-    int *sRowIn = reinterpret_cast<int *>(sGv + (nG ? dG : 0) * kTileB), *sRowBase = sRowIn + nIn;
+    int *sRowIn = reinterpret_cast<int *>(sGv + (extra ? dG : 0) * kTileB), *sRowBase = sRowIn + nIn;
     for (int r = threadIdx.x; r < nIn; r += blockDim.x) sRowIn[r] = (int)rowIn(r);
     for (int r = threadIdx.x; r < nBase; r += blockDim.x) sRowBase[r] = (int)rowBase(r);
     __syncthreads();
@@ -312,24 +314,32 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, kOpCtasPerSm<T>) k_lstar_b
             A.out[o] = val;
             if (A.outR) A.outR[o] = BASE(rb) - val;
         };
-        if (nG) {  // Gamma' times the Gamma rows of III (or V) into shared memory (constraints.cuh:272-285, 410-425)
+        if (extra) {  // Gamma' times the Gamma rows of III or V (constraints.cuh:272-285, 410-425), plus the
+                      // linear-cost gradients times IV / VI (costs.cuh:274-292), into shared memory
             T accG[kMaxTasks][kRT];
             zeroAcc(accG);
             const int rg = nonleaf ? rIIIg : dVI + nId;
-            gemv(accG, sGT, dG, nG, warp, [&](int k) { return IN(rg + k); });
+            if (nG) gemv(accG, sGT, dG, nG, warp, [&](int k) { return IN(rg + k); });
     #pragma unroll
             for (int q = 0; q < kMaxTasks; q++) {
                 const int r0 = (warp + q * kTileWarps) * kRT;
     #pragma unroll
-                for (int t = 0; t < kRT; t++)
-                    if (r0 + t < dG) sGv[(r0 + t) * kTileB + lane] = accG[q][t];
+                for (int t = 0; t < kRT; t++) {
+                    const int r = r0 + t;
+                    if (r >= dG) continue;
+                    T v = accG[q][t];
+                    if (nonleaf && linNl)
+                        for (int jj = 0; jj < nc; jj++) v += __ldg(P.grad + (size_t)(c0 + jj) * nxu + r) * IN(jj * dIV);
+                    if (!nonleaf && linL) v += __ldg(P.lGrad + r) * IN(0);
+                    sGv[r * kTileB + lane] = v;
+                }
             }
             __syncthreads();
         }
-        // constraint part of x_i / u_i (row r of [x; u]): identity rows and Gamma' rows
+        // constraint and linear-cost part of x_i / u_i (row r of [x; u])
         auto conPart = [&](int r, int rId) -> T {
             T v = nId ? IN(rId + r) : T(0);
-            if (nG) v += sGv[r * kTileB + lane];
+            if (extra) v += sGv[r * kTileB + lane];
             return v;
         };
         T accX[kMaxTasks][kRT], accU[kMaxTasks][kRT];
@@ -338,12 +348,6 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, kOpCtasPerSm<T>) k_lstar_b
         if (nonleaf) {
             const bool qpl = D.costNl == kCostQuadraticPlusLinear;
             const int sx = warp, su = slotFrom(warp, tasksOf(nx));  // x and u blocks on different warps
-            auto linPart = [&](int r) -> T {  // linear costs: sum over children of g_j[r] * IV_j
-                T v = 0;
-                if (linNl)
-                    for (int jj = 0; jj < nc; jj++) v += __ldg(P.grad + (size_t)(c0 + jj) * nxu + r) * IN(jj * dIV);
-                return v;
-            };
             for (int jj = 0; jj < nc && !linNl; jj++) {
                 const int r0 = jj * dIV;
                 const T *m = sMat + jj * perChild;
@@ -360,8 +364,8 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, kOpCtasPerSm<T>) k_lstar_b
                 const int rx0 = (sx + q * kTileWarps) * kRT, ru0 = (su + q * kTileWarps) * kRT;
     #pragma unroll
                 for (int t = 0; t < kRT; t++) {
-                    if (rx0 + t < nx) EMIT(rx0 + t, accX[q][t] + conPart(rx0 + t, rIII) + linPart(rx0 + t));
-                    if (ru0 + t < nu) EMIT(nx + ru0 + t, accU[q][t] + conPart(nx + ru0 + t, rIII) + linPart(nx + ru0 + t));
+                    if (rx0 + t < nx) EMIT(rx0 + t, accX[q][t] + conPart(rx0 + t, rIII));
+                    if (ru0 + t < nu) EMIT(nx + ru0 + t, accU[q][t] + conPart(nx + ru0 + t, rIII));
                 }
             }
             // y_i, the children's t and s, and the AVaR kernel projection (cache.cuh:650-676): entry
@@ -428,7 +432,7 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, kOpCtasPerSm<T>) k_lstar_b
     #pragma unroll
                 for (int t = 0; t < kRT; t++) {
                     const int r = r0 + t;
-                    if (r < nx) EMIT(r, accX[q][t] + conPart(r, dVI) + (linL ? __ldg(P.lGrad + r) * IN(0) : T(0)));
+                    if (r < nx) EMIT(r, accX[q][t] + conPart(r, dVI));
                 }
             }
         }
