@@ -89,6 +89,14 @@ int spock_solve(spock_solver s, int algo, const double *x0, long count, const do
  * element-major (x0[c * batch + b]); results stay on the device until read. */
 int spock_solve_device(spock_solver s, int algo, const void *x0_device, int *statuses, long *iters);
 
+/* Mixed batches (instances of different trees and dimensions, one solver per problem): cold-start
+ * solves of `count` distinct solvers at once, one host thread each, every solver on its own CUDA
+ * stream so the GPU runs them concurrently; returns when all have stopped.  x0s[i] holds
+ * x0counts[i] rows for solver i (as spock_solve); statuses[i] / iters[i] (batch entries each) may be
+ * NULL, as may statuses / iters.  No reference counterpart. */
+int spock_solve_group(long count, spock_solver *solvers, int algo, const double *const *x0s, const long *x0counts,
+                      int *const *statuses, long *const *iters);
+
 /* Re-solve every instance warm-started from the solver's current iterate -- the solution of
  * the previous solve, still on the device -- with new initial states: the reference's
  * previousSolution warm start (cache.cuh:611-632) for a control loop that re-solves as the state

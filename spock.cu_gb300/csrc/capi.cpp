@@ -6,6 +6,8 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "capi_internal.hpp"
 #include "engine.cuh"
@@ -191,6 +193,39 @@ int spock_offline_dynamics(spock_problem pp, int device, int replace, double *P,
                             hp.Pe[j * nx + r] += hp.P[j * nx * nx + col * nx + r] * hp.e[j * nx + col];
             }
         }
+    });
+}
+
+int spock_solve_group(long count, spock_solver *solvers, int algo, const double *const *x0s, const long *x0counts,
+                      int *const *statuses, long *const *iters) {
+    return guard([&] {
+        if (count < 1 || !solvers || !x0s || !x0counts) throw std::invalid_argument("[solveGroup] bad arguments");
+        if (algo != SPOCK_ALGO_SPOCK && algo != SPOCK_ALGO_CP) throw std::invalid_argument("[Cache] unknown algorithm");
+        for (long i = 0; i < count; i++) {
+            solver(solvers[i]);
+            need(x0s[i], "x0");
+            for (long j = 0; j < i; j++)
+                if (solvers[j] == solvers[i]) throw std::invalid_argument("[solveGroup] a solver appears twice");
+        }
+        std::vector<std::string> errors((size_t)count);
+        std::vector<std::thread> threads;
+        threads.reserve((size_t)count);
+        for (long i = 0; i < count; i++)
+            threads.emplace_back([&, i] {
+                try {
+                    auto *s = solver(solvers[i]);
+                    if (cudaSetDevice(s->eng->device()) != cudaSuccess) throw std::runtime_error("cudaSetDevice failed");
+                    s->eng->setInitialStates(x0s[i], x0counts[i]);
+                    s->eng->run(algo == SPOCK_ALGO_SPOCK ? spock::kSpock : spock::kCp, false);
+                    finishSolve(s, statuses ? statuses[i] : nullptr, iters ? iters[i] : nullptr);
+                } catch (const std::exception &e) {
+                    errors[(size_t)i] = e.what();
+                }
+            });
+        for (auto &t : threads) t.join();
+        for (long i = 0; i < count; i++)
+            if (!errors[(size_t)i].empty())
+                throw std::invalid_argument("[solveGroup] solver " + std::to_string(i) + ": " + errors[(size_t)i]);
     });
 }
 

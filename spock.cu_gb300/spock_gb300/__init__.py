@@ -75,6 +75,8 @@ _SIGS = {
     "spock_counters_all": (ctypes.c_int, [_vp, _lp]),
     "spock_set_tuning": (ctypes.c_int, [_vp, _ip]),
     "spock_copy_iterate": (ctypes.c_int, [_vp, _vp]),
+    "spock_solve_group": (ctypes.c_int, [ctypes.c_long, ctypes.POINTER(_vp), ctypes.c_int, ctypes.POINTER(_dp), _lp,
+                                         ctypes.POINTER(_ip), ctypes.POINTER(_lp)]),
     "spock_set_iterate_device": (ctypes.c_int, [_vp, _vp, ctypes.c_int]),
     "spock_mlp_create": (ctypes.c_int, [_ip, ctypes.c_int, ctypes.POINTER(_vp)]),
     "spock_mlp_free": (None, [_vp]),
@@ -440,3 +442,22 @@ class Cache:
         ms = ctypes.c_double()
         _check(lib().spock_round_time(self._h, rounds, ctypes.byref(ms)))
         return ms.value
+
+
+def solve_group(caches, x0s, algo=0):
+    """Mixed batch: cold-start solves of several solvers (different problems) at once, one host
+    thread and CUDA stream each.  x0s[i] has rows for caches[i].  Returns the status arrays."""
+    n = len(caches)
+    if n != len(x0s):
+        raise ValueError("one x0 array per solver")
+    xs = [np.ascontiguousarray(np.atleast_2d(np.asarray(x, dtype=np.float64))) for x in x0s]
+    for c, x in zip(caches, xs):
+        if x.shape[1] != c._tree.numStates():
+            raise ValueError("[initialiseState] wrong number of states")
+    hs = (_vp * n)(*[c._h for c in caches])
+    xp = (_dp * n)(*[_p(x) for x in xs])
+    cnt = np.array([x.shape[0] for x in xs], dtype=np.int64)
+    sp = (_ip * n)(*[c._status.ctypes.data_as(_ip) for c in caches])
+    ip = (_lp * n)(*[c._iters.ctypes.data_as(_lp) for c in caches])
+    _check(lib().spock_solve_group(n, hs, algo, xp, cnt.ctypes.data_as(_lp), sp, ip))
+    return [c._status.copy() for c in caches]

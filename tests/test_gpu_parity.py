@@ -373,3 +373,27 @@ def test_instance_compaction(oracle_lib):
     keep = np.ones(128, bool)
     keep[::4] = False
     assert np.abs(c.solutions()[keep] - z[keep]).max() <= 1e-6 * max(1., np.abs(z).max())
+
+
+def test_mixed_batch_solve_group(oracle_lib):
+    """Mixed batch (instances of different trees and dimensions): three problems solved at once by
+    spock_solve_group, one host thread and stream each, give exactly the solutions and iteration
+    counts of the same solves run one after another."""
+    specs = [("reftest", 64, 1, np.full((1, 3), 1.1)), ("cfg1", 32, 40, None), ("qpl", 64, 8, None)]
+    rng = np.random.default_rng(51)
+    caches, alone, x0s = [], [], []
+    for case, prec, batch, x0 in specs:
+        path = os.path.join(GOLDEN, case)
+        P = oracle_lib.Problem(path)
+        x = x0 if x0 is not None else rng.uniform(-1, 1, (batch, P.nx))
+        x0s.append(x)
+        t, d, c = make(path, prec, batch=batch, tol=1e-3, max_iters=3000)
+        caches.append(c)
+        t2, d2, c2 = make(path, prec, batch=batch, tol=1e-3, max_iters=3000)
+        c2.runSpockBatch(x)
+        alone.append(c2)
+    sts = sg.solve_group(caches, x0s)
+    for c, c2, st in zip(caches, alone, sts):
+        assert (st == c2.statuses()).all() and (st == 0).all()
+        assert (c.solveIters() == c2.solveIters()).all()
+        assert np.array_equal(c.solutions(), c2.solutions())

@@ -73,15 +73,15 @@ def test_mlp_forward_and_gradients_match_numpy():
 
 
 def test_learned_warm_start_end_to_end(oracle_lib):
-    """Fit PCA + MLP on 256 solved instances of the config-1 problem, predict warm starts for 64
-    new initial states: every warm-started instance converges to the same first input as a cold
-    solve (the warm start changes the path, not the answer)."""
+    """Fit PCA + MLP on 256 solved instances of the reference's test problem, predict warm starts
+    for 64 new initial states: every warm-started instance converges to the same first input as
+    a cold solve (the warm start changes the path, not the answer)."""
     import torch
     from spock_gb300.warmstart import PcaMlpWarmStart
-    path = os.path.join(GOLDEN, "cfg1")
+    path = os.path.join(GOLDEN, "reftest")
     P = oracle_lib.Problem(path)
     rng = np.random.default_rng(9)
-    xtr = rng.uniform(-1, 1, (256, P.nx))
+    xtr = 1.1 + rng.uniform(-.05, .05, (256, P.nx))
     t = sg.ScenarioTree(path)
     d = sg.ProblemData(t)
     c = sg.CacheBuilder(t, d).tol(1e-4).andersonBuffer(3).maxIters(20000).precision(64).batch(256).build()
@@ -90,7 +90,7 @@ def test_learned_warm_start_end_to_end(oracle_lib):
     ws = PcaMlpWarmStart(k=8, hidden=64, seed=2)
     losses = ws.fit(xtr, zs, epochs=60, batch=64, lr=3e-3)
     assert losses[-1] < losses[0]
-    xte = rng.uniform(-1, 1, (64, P.nx))
+    xte = 1.1 + rng.uniform(-.05, .05, (64, P.nx))
     cw = sg.CacheBuilder(t, d).tol(1e-4).andersonBuffer(3).maxIters(20000).precision(64).batch(64).build()
     ws.warm_start(cw, xte)
     assert (cw.resolveBatch(xte) == 0).all()
