@@ -58,11 +58,27 @@ def dist_info():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def instance_slice(count, rank):
+    """Replicas: rank r solves its own instances r*count .. (r+1)*count-1 (no data exchange)."""
+    return slice(rank * count, (rank + 1) * count)
+
+
+def max_over_ranks(seconds, world):
+    """The job's time: the slowest rank's (a gloo or NCCL all-reduce when world > 1)."""
+    if world <= 1:
+        return float(seconds)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(seconds)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t[0])
+
+
 def workload(seed, count, rank=0):
-    """Problem folder and this rank's initial states (instances rank*count .. (rank+1)*count-1)."""
+    """Problem folder and this rank's initial states."""
     from spock_gb300 import configs
     path, x0 = configs.cached("config2", PROBLEM_DIR, seed=seed, count=count * (rank + 1), cost_scale=COST_SCALE)
-    return path, np.ascontiguousarray(x0[rank * count:(rank + 1) * count])
+    return path, np.ascontiguousarray(x0[instance_slice(count, rank)])
 
 
 def trajectory(x0s, steps, seed, rank=0):
@@ -288,12 +304,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     clk = clocks.stop()
-    t_dev = e0.elapsed_time(e1) / 1e3
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_dev])
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_dev = float(tt[0])
+    t_dev = max_over_ranks(e0.elapsed_time(e1) / 1e3, world)
     st_all, it_all, calls_all = np.concatenate(statuses), np.concatenate(iters), np.concatenate(calls)
     conv = st_all == 0
     value = B * world * args.steps / t_dev
