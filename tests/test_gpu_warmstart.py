@@ -81,7 +81,8 @@ def test_learned_warm_start_end_to_end(oracle_lib):
     path = os.path.join(GOLDEN, "reftest")
     P = oracle_lib.Problem(path)
     rng = np.random.default_rng(9)
-    xtr = 1.1 + rng.uniform(-.05, .05, (256, P.nx))
+    # x0 = 1.1 + s (1, 1, 1), s in [-0.05, 0.05]: feasible for the problem's terminal box |x| <= 0.1
+    xtr = 1.1 + rng.uniform(-.05, .05, (256, 1)) * np.ones(P.nx)
     t = sg.ScenarioTree(path)
     d = sg.ProblemData(t)
     c = sg.CacheBuilder(t, d).tol(1e-4).andersonBuffer(3).maxIters(20000).precision(64).batch(256).build()
@@ -90,7 +91,7 @@ def test_learned_warm_start_end_to_end(oracle_lib):
     ws = PcaMlpWarmStart(k=8, hidden=64, seed=2)
     losses = ws.fit(xtr, zs, epochs=60, batch=64, lr=3e-3)
     assert losses[-1] < losses[0]
-    xte = 1.1 + rng.uniform(-.05, .05, (64, P.nx))
+    xte = 1.1 + rng.uniform(-.05, .05, (64, 1)) * np.ones(P.nx)
     cw = sg.CacheBuilder(t, d).tol(1e-4).andersonBuffer(3).maxIters(20000).precision(64).batch(64).build()
     ws.warm_start(cw, xte)
     assert (cw.resolveBatch(xte) == 0).all()
