@@ -152,6 +152,11 @@ int spock_run_stats(spock_solver s, long *rounds, long *launches, long *compacti
  * double-buffered, dynamics-sweep tiles per CTA (0 when the small-batch kernels run)}.  No
  * reference counterpart. */
 int spock_tuning(spock_solver s, int *out5);
+/* The step size gamma = 0.99 / ||L|| that Problem.__get_step_size computes with ARPACK
+ * (api/python/spock/problem.py:402-417), here from `iters` steps of the power iteration on
+ * lambda_max(L* L) run on the GPU with the solver's own L and L* kernels; outputs may be NULL. */
+int spock_step_size(spock_solver s, int iters, double *norm_sq, double *step);
+
 /* Override the autotuner: in3 = {L* tiles per CTA, L tiles per CTA, dynamics-sweep tiles per CTA},
  * each 1, 2, 4 or 8 (double-buffered where two tiles fit in shared memory).  No effect on the
  * small-batch kernels.  No reference counterpart. */

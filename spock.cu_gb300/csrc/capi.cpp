@@ -2,6 +2,7 @@
 // they become SPOCK_E_* codes with the message kept for spock_last_error().
 #include "../../include/spock_gb300.h"
 
+#include <cmath>
 #include <cstring>
 #include <memory>
 #include <stdexcept>
@@ -412,6 +413,15 @@ int spock_tuning(spock_solver sv, int *out5) {
     return guard([&] {
         if (!out5) throw std::invalid_argument("[spock_tuning] null output");
         solver(sv)->eng->tuning(out5);
+    });
+}
+
+int spock_step_size(spock_solver sv, int iters, double *norm_sq, double *step) {
+    return guard([&] {
+        if (iters < 1) throw std::invalid_argument("[stepSize] iters must be positive");
+        const double lam = solver(sv)->eng->normLsq(iters);
+        if (norm_sq) *norm_sq = lam;
+        if (step) *step = 0.99 / std::sqrt(lam);
     });
 }
 

@@ -502,6 +502,22 @@ __global__ void k_tile_flags(const int *status, int B, int *tileLive) {
     if ((threadIdx.x & 31) == 0 && b < B) tileLive[b >> 5] = any != 0;
 }
 
+// sum of squares of x[0 .. n) into *out (FP64)
+template <typename T>
+__global__ void k_sumsq(const T *x, size_t n, double *out) {
+    double s = 0;
+    for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < n; o += (size_t)gridDim.x * blockDim.x)
+        s += (double)x[o] * (double)x[o];
+    for (int q = 16; q > 0; q >>= 1) s += __shfl_xor_sync(0xffffffffu, s, q);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
+}
+
+template <typename T>
+__global__ void k_scale(T *x, size_t n, double f) {
+    for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < n; o += (size_t)gridDim.x * blockDim.x)
+        x[o] = (T)((double)x[o] * f);
+}
+
 __global__ void k_count_active(const int *status, int B, int *out) {
     __shared__ int cnt;
     if (threadIdx.x == 0) cnt = 0;
@@ -738,6 +754,42 @@ public:
         uploadSlice(R_, z, 0, D_.sZ);
         applyMres();
         downloadSlice(MR_, mz, 0, D_.sZ);
+    }
+
+    double normLsq(int iters) override {  // problem.py:402-417 computes the same with ARPACK
+        allLive();
+        const size_t np = (size_t)D_.sPrim * B_;
+        fill(W1_, (size_t)D_.sZ * B_, T(0));
+        fill(W1_, np, T(1));
+        double *dsum = nullptr;
+        CK(cudaMalloc(&dsum, sizeof(double)));
+        double lam = 0, nrm2 = 0;
+        auto norm2 = [&]() {
+            CK(cudaMemsetAsync(dsum, 0, sizeof(double), stream_));
+            k_sumsq<T><<<(int)std::min<size_t>((np + 255) / 256, 152 * 8), 256, 0, stream_>>>(W1_, np, dsum);
+            CK(cudaGetLastError());
+            double h = 0;
+            CK(cudaMemcpyAsync(&h, dsum, sizeof(double), cudaMemcpyDeviceToHost, stream_));
+            CK(cudaStreamSynchronize(stream_));
+            return h;
+        };
+        nrm2 = norm2();
+        k_scale<T><<<(int)std::min<size_t>((np + 255) / 256, 152 * 8), 256, 0, stream_>>>(W1_, np, 1. / std::sqrt(nrm2));
+        for (int it = 0; it < iters; it++) {
+            OpArgs<T> A = blankArgs();
+            A.in1 = W1_; A.a1 = 1; A.cL = 1; A.out = W2_;  // W2 dual = L p
+            launchLop<2>(A);
+            OpArgs<T> A2 = blankArgs();
+            A2.in1 = W2_; A2.a1 = 1; A2.cL = 1; A2.out = W1_;  // W1 prim = L* L p
+            launchLstar<2>(A2);
+            nrm2 = norm2();
+            lam = std::sqrt(nrm2);  // ||L* L p|| with ||p|| = 1
+            if (!(lam > 0)) break;
+            k_scale<T><<<(int)std::min<size_t>((np + 255) / 256, 152 * 8), 256, 0, stream_>>>(W1_, np, 1. / lam);
+            CK(cudaGetLastError());
+        }
+        cudaFree(dsum);
+        return lam;  // every instance holds the same vector, and the norm runs over all of them
     }
 
     void setTuning(int lstar, int lop, int dyn) override {

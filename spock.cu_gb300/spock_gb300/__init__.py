@@ -74,6 +74,7 @@ _SIGS = {
     "spock_tuning": (ctypes.c_int, [_vp, _ip]),
     "spock_counters_all": (ctypes.c_int, [_vp, _lp]),
     "spock_set_tuning": (ctypes.c_int, [_vp, _ip]),
+    "spock_step_size": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp]),
     "spock_copy_iterate": (ctypes.c_int, [_vp, _vp]),
     "spock_solve_group": (ctypes.c_int, [ctypes.c_long, ctypes.POINTER(_vp), ctypes.c_int, ctypes.POINTER(_dp), _lp,
                                          ctypes.POINTER(_ip), ctypes.POINTER(_lp)]),
@@ -413,6 +414,12 @@ class Cache:
         _check(lib().spock_tuning(self._h, out.ctypes.data_as(_ip)))
         return dict(zip(["lstar_tiles_per_cta", "lstar_double_buffer", "lop_tiles_per_cta", "lop_double_buffer",
                          "dyn_tiles_per_cta"], out.tolist()))
+
+    def stepSize(self, iters=5000):
+        """(||L||^2, 0.99 / ||L||) by the power iteration on the GPU (problem.py:402-417)."""
+        lam, step = ctypes.c_double(), ctypes.c_double()
+        _check(lib().spock_step_size(self._h, int(iters), ctypes.byref(lam), ctypes.byref(step)))
+        return lam.value, step.value
 
     def setTuning(self, lstar, lop, dyn):
         """Override the autotuner's tiles per CTA (1, 2, 4 or 8) for L*, L and the dynamics sweep."""

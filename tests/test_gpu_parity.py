@@ -16,6 +16,7 @@ import spock_gb300 as sg
 pytestmark = pytest.mark.gpu
 
 CASES = ["reftest", "cfg1", "qpl"]
+GOLDEN_CASES_ALL = ["reftest", "cfg1", "qpl", "affpoly"]
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -397,3 +398,15 @@ def test_mixed_batch_solve_group(oracle_lib):
         assert (st == c2.statuses()).all() and (st == 0).all()
         assert (c.solveIters() == c2.solveIters()).all()
         assert np.array_equal(c.solutions(), c2.solutions())
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES_ALL)
+def test_step_size_on_gpu(case):
+    """spock_step_size: 0.99 / ||L|| from the power iteration on the GPU (FP64, the library's own L
+    and L* kernels) matches the step size the reference factory wrote (ARPACK, problem.py:402-417)."""
+    import json
+    path = os.path.join(GOLDEN, case)
+    ref = json.load(open(os.path.join(path, "data.json")))["stepSize"]
+    t, d, c = make(path, 64)
+    lam, step = c.stepSize(20000)
+    assert abs(step - ref) <= 1e-6 * ref
