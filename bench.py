@@ -105,10 +105,10 @@ class Clocks:
     """nvidia-smi sampling during the timed region."""
 
     def __init__(self, index):
+        import tempfile
         self.proc = None
         self.index = index
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{index}.csv") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) \
-            else f"/tmp/spock_clocks_{index}.csv"
+        self.path = os.path.join(tempfile.gettempdir(), f"spock_clocks_{os.getpid()}_{index}.csv")
 
     def start(self):
         try:
