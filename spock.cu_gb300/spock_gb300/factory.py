@@ -235,6 +235,21 @@ class Polyhedron:
         self.lb, self.ub = np.asarray(lb, float).ravel(), np.asarray(ub, float).ravel()
 
 
+class PolyhedronWithIdentity:
+    """lb <= [I; Gamma] z <= ub from a Rectangle and a Polyhedron (build.py:1025-1096); the dual
+    block holds the identity rows of every node, then the Gamma rows of every node
+    (build.py:1050-1070)."""
+    kind = "polyhedronWithIdentity"
+
+    def __init__(self, rect, poly):
+        if not isinstance(rect, Rectangle) or not isinstance(poly, Polyhedron):
+            raise TypeError("PolyhedronWithIdentity takes a Rectangle and a Polyhedron")
+        if poly.G.shape[1] != rect.lb.size:
+            raise ValueError("PolyhedronWithIdentity: Gamma and the rectangle differ in dimension")
+        self.rect, self.poly = rect, poly
+        self.lb, self.ub, self.G, self.glb, self.gub = rect.lb, rect.ub, poly.G, poly.lb, poly.ub
+
+
 class AVaR:
     """AVaR_alpha: E = [alpha I; -I; 1'], b = [p; 0; 1] (build.py:1160-1193)."""
     kind = "avar"
@@ -488,6 +503,8 @@ class Problem:
             return (con.lb * scale, con.ub * scale, con.radius * su[0])
         if con.kind == "polyhedron":
             return (con.G / scale[None, :], con.lb, con.ub)
+        if con.kind == "polyhedronWithIdentity":
+            return (con.G / scale[None, :], con.glb, con.gub, con.lb * scale, con.ub * scale)
         raise ValueError("constraint kind %s not supported by this factory" % con.kind)
 
     def _offline_dynamics(self):
@@ -520,9 +537,11 @@ class Problem:
         n, nnl, nl = t.num_nodes, t.num_nonleaf_nodes, t.num_leaf_nodes
         self.size_prim = (nu + self.y_dim) * nnl + (nx + 2) * n
         d3 = {"no": 0, "rectangle": nx + nu, "rectangleInputBall": nx + nu}.get(self.nl_con.kind, None)
-        d3 = self.nl_bounds[0].shape[0] if d3 is None else d3
+        d3 = self.nl_bounds[0].shape[0] + (nx + nu if self.nl_con.kind == "polyhedronWithIdentity" else 0) \
+            if d3 is None else d3
         d5 = {"no": 0, "rectangle": nx}.get(self.l_con.kind, None)
-        d5 = self.l_bounds[0].shape[0] if d5 is None else d5
+        d5 = self.l_bounds[0].shape[0] + (nx if self.l_con.kind == "polyhedronWithIdentity" else 0) \
+            if d5 is None else d5
         d4 = 2 if self.cost_kind == "linear" else nx + nu + 2
         d6 = 2 if self.leaf_kind == "linear" else nx + 2
         self.size_dual = self.y_dim * nnl + nnl + d3 * nnl + d4 * n + d5 * nl + d6 * nl
@@ -549,6 +568,8 @@ class Problem:
             out.append(xu.ravel())
         elif self.nl_con.kind == "polyhedron":
             out.append((xu @ self.nl_bounds[0].T).ravel())
+        elif self.nl_con.kind == "polyhedronWithIdentity":
+            out += [xu.ravel(), (xu @ self.nl_bounds[0].T).ravel()]
         anc = t.ancestors[1:]
         xa, ua = x[anc], u[anc]
         if self.cost_kind == "linear":
@@ -570,6 +591,8 @@ class Problem:
             out.append(xl.ravel())
         elif self.l_con.kind == "polyhedron":
             out.append((xl @ self.l_bounds[0].T).ravel())
+        elif self.l_con.kind == "polyhedronWithIdentity":
+            out += [xl.ravel(), (xl @ self.l_bounds[0].T).ravel()]
         if self.leaf_kind == "linear":
             out += [xl @ self.lq, sl]
         else:
@@ -603,6 +626,12 @@ class Problem:
             xu = III @ G
             x[:nnl] = xu[:, :nx]
             u[:] = xu[:, nx:]
+        elif self.nl_con.kind == "polyhedronWithIdentity":
+            G = self.nl_bounds[0]
+            xu = d[o:o + (nx + nu) * nnl].reshape(nnl, nx + nu).copy(); o += (nx + nu) * nnl
+            xu += d[o:o + G.shape[0] * nnl].reshape(nnl, G.shape[0]) @ G; o += G.shape[0] * nnl
+            x[:nnl] = xu[:, :nx]
+            u[:] = xu[:, nx:]
         anc = t.ancestors[1:]
         if self.cost_kind == "linear":
             s4 = d[o:o + n]; o += n
@@ -625,6 +654,10 @@ class Problem:
         elif self.l_con.kind == "polyhedron":
             G = self.l_bounds[0]
             x[nnl:] = d[o:o + G.shape[0] * nl].reshape(nl, G.shape[0]) @ G; o += G.shape[0] * nl
+        elif self.l_con.kind == "polyhedronWithIdentity":
+            G = self.l_bounds[0]
+            x[nnl:] = d[o:o + nx * nl].reshape(nl, nx); o += nx * nl
+            x[nnl:] += d[o:o + G.shape[0] * nl].reshape(nl, G.shape[0]) @ G; o += G.shape[0] * nl
         if self.leaf_kind == "linear":
             x[nnl:] += d[o:o + nl, None] * self.lq[None, :]; o += nl
             s[nnl:] = d[o:o + nl]
@@ -690,10 +723,13 @@ class Problem:
                 w(txt + "IUB", bnd[1])
                 if con.kind == "rectangleInputBall":
                     w(txt + "Radius", np.array([bnd[2]]))
-            elif con.kind == "polyhedron":
+            elif con.kind in ("polyhedron", "polyhedronWithIdentity"):
                 w(txt + "Gamma", bnd[0])
                 w(txt + "GLB", bnd[1])
                 w(txt + "GUB", bnd[2])
+                if con.kind == "polyhedronWithIdentity":
+                    w(txt + "ILB", bnd[3])
+                    w(txt + "IUB", bnd[4])
         meta = {
             "numEvents": int(t.num_events), "numNonleafNodes": int(t.num_nonleaf_nodes),
             "numNodes": int(n), "numStages": int(t.num_stages), "numStates": nx, "numInputs": nu,

@@ -124,3 +124,50 @@ def test_config_sizes(tmp_path):
     assert (t2.num_nodes, t2.num_leaf_nodes) == (607, 81)
     t3 = F.IidProcess(np.ones(5) / 5, 8, 3).build()
     assert (t3.num_nodes, t3.num_leaf_nodes) == (781, 125)
+
+
+def build_polyid(path, preconditioning=True):
+    """Polyhedron-with-identity constraints on nonleaf and leaf nodes (build.py:1025-1096):
+    the reference's Python class cannot write fixtures (its assign_dual reads the Gamma block
+    from the identity block's offset), so this case is checked against the oracle reading the
+    files written here."""
+    rng = np.random.default_rng(5)
+    ne, nx, nu = 2, 3, 2
+    tree = F.MarkovChain(np.array([[.7, .3], [.4, .6]]), np.array([.5, .5]), 3, 2).build()
+    dyn = [F.Dynamics(np.eye(nx) + .1 * rng.standard_normal((nx, nx)), rng.standard_normal((nx, nu)))
+           for _ in range(ne)]
+    Q, R = np.diag(rng.uniform(1., 5., nx)), np.diag(rng.uniform(.1, 1., nu))
+    lb = np.concatenate((-4. * np.ones(nx), -2. * np.ones(nu)))
+    nl = F.PolyhedronWithIdentity(F.Rectangle(lb, -lb), F.Polyhedron(rng.standard_normal((2, nx + nu)),
+                                                                     -np.ones(2), np.ones(2)))
+    lf = F.PolyhedronWithIdentity(F.Rectangle(-4. * np.ones(nx), 4. * np.ones(nx)),
+                                  F.Polyhedron(rng.standard_normal((3, nx)), -2. * np.ones(3), 2. * np.ones(3)))
+    return (F.Factory(tree, nx, nu).with_dynamics_events(dyn).with_cost_nonleaf(F.CostQuadratic(Q, R))
+            .with_cost_leaf(F.CostQuadratic(Q.copy(), leaf=True)).with_constraint_nonleaf(nl)
+            .with_constraint_leaf(lf).with_risk(F.AVaR(.9)).with_preconditioning(preconditioning)
+            .generate_problem(path))
+
+
+@pytest.mark.parametrize("preconditioning", [False, True])
+def test_polyhedron_with_identity(oracle_lib, tmp_path, preconditioning):
+    """The factory's L, L* and step size for [I; Gamma] constraints equal the oracle's on the
+    written problem; the dual block is the identity rows of every node, then the Gamma rows."""
+    path = str(tmp_path) + "/"
+    prob = build_polyid(path, preconditioning)
+    P = oracle_lib.Problem(path)
+    meta = json.load(open(path + "data.json"))
+    assert meta["constraint"] == {"nonleaf": "polyhedronWithIdentity", "leaf": "polyhedronWithIdentity"}
+    rng = np.random.default_rng(1)
+    x, y = rng.standard_normal(P.size_prim), rng.standard_normal(P.size_dual)
+    assert np.allclose(prob.op(x), P.op(x), rtol=0, atol=1e-12 * np.abs(P.op(x)).max())
+    assert np.allclose(prob.adj(y), P.adj(y), rtol=0, atol=1e-12 * np.abs(P.adj(y)).max())
+    assert abs(y @ P.op(x) - P.adj(y) @ x) <= 1e-10 * abs(y @ P.op(x))
+    assert abs(.99 / np.sqrt(P.norm_L_sq(20000)) - P.step) <= 1e-8 * P.step
+    # identity rows of node 1 hold [x_1; u_1] (scaled); rows after all identity rows hold Gamma
+    nnl, nx, nu = prob.tree.num_nonleaf_nodes, 3, 2
+    e = np.zeros(P.size_prim)
+    e[nu * nnl + nx + 0] = 1.                     # x_1[0]
+    d = P.op(e)
+    off = prob.y_dim * nnl + nnl                  # after the risk rows and s - b'y
+    assert d[off + (nx + nu) * 1 + 0] == 1.
+    assert np.count_nonzero(d[off:off + (nx + nu) * nnl]) == 1

@@ -410,3 +410,30 @@ def test_step_size_on_gpu(case):
     t, d, c = make(path, 64)
     lam, step = c.stepSize(20000)
     assert abs(step - ref) <= 1e-6 * ref
+
+
+@pytest.mark.parametrize("batch", BATCHES)
+def test_polyhedron_with_identity(oracle_lib, tmp_path, batch):
+    """[I; Gamma] constraints on nonleaf and leaf nodes (constraints.cuh:296-426), preconditioned:
+    L, L* and the T step against the oracle (FP64 1e-10, FP32 1e-4), and an FP64 SPOCK solve
+    with the oracle's u_0."""
+    from test_factory import build_polyid
+    path = str(tmp_path) + "/"
+    build_polyid(path)
+    P = oracle_lib.Problem(path)
+    rng = np.random.default_rng(43)
+    x0 = rng.uniform(-.5, .5, P.nx)
+    p, q = rng.standard_normal(P.size_prim), rng.standard_normal(P.size_dual)
+    for prec, tol in [(64, 1e-10), (32, 1e-4)]:
+        t, d, c = make(path, prec, batch=batch)
+        assert rel(c.op(p), P.op(p)) < tol
+        assert rel(c.adj(q), P.adj(q)) < tol
+        for _ in range(3):
+            z = 3 * rng.standard_normal(P.size)
+            assert rel(c.cpStep(x0, z), P.cp_step(x0 * P.scaling[:P.nx], z)) < tol
+    t, d, c = make(path, 64, batch=batch, tol=1e-8, max_iters=20000)
+    assert c.runSpock(x0) == 0
+    z, s = P.run(x0, oracle_lib.options(tol=1e-8, max_iters=20000), "spock")
+    assert s.status == 0
+    u_ref = P.states_inputs(z)[1][:P.nu]
+    assert np.abs(c.inputs()[:P.nu] - u_ref).max() <= 1e-5 * max(1., np.abs(u_ref).max())
