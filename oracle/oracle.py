@@ -78,8 +78,20 @@ def lib():
         L.or_offline_kernel.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_long, _dp]
         L.or_norm_L_sq.restype = ctypes.c_double
         L.or_norm_L_sq.argtypes = [ctypes.c_void_p, ctypes.c_long]
+        L.or_set_emulation.argtypes = [ctypes.c_int]
         _lib = L
     return _lib
+
+
+# FP32 emulation modes (spock_oracle.h): problem data, matvec accumulation, vector storage,
+# Anderson normal equations, and the two remedies for the forward rollout.
+EMU_DATA, EMU_ACC, EMU_VEC, EMU_GRAM, EMU_FWD64, EMU_FWDC = 1, 2, 4, 8, 16, 32
+EMU_GPU_FP32 = EMU_DATA | EMU_ACC | EMU_VEC | EMU_GRAM
+
+
+def set_emulation(mode):
+    """Process-wide FP32 emulation mode (0 = plain FP64); set it before loading a Problem."""
+    lib().or_set_emulation(int(mode))
 
 
 def _p(a):

@@ -58,6 +58,15 @@ struct OrProblem {
 };
 
 static char g_err[2048];
+
+/* FP32 emulation mode (spock_oracle.h, OR_EMU_*); 0 keeps every operation in double. */
+static int g_emu = 0;
+void or_set_emulation(int mode) { g_emu = mode; }
+static void r32(double *v, long n) {
+    for (long i = 0; i < n; i++) v[i] = (double)(float)v[i];
+}
+#define EMU_VEC(v, n) do { if (g_emu & OR_EMU_VEC) r32((v), (n)); } while (0)
+
 const char *or_last_error(void) { return g_err; }
 
 #define FAIL(...) do { snprintf(g_err, sizeof g_err, __VA_ARGS__); goto fail; } while (0)
@@ -94,6 +103,7 @@ static long read_bt(const char *dir, const char *name, char kind, void **out, lo
     if (kind == 'd') {
         double *a = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
         memcpy(a, buf + 24, (size_t)n * 8);
+        if (g_emu & OR_EMU_DATA) r32(a, n);
         *out = a;
     } else {
         long *a = (long *)malloc(sizeof(long) * (size_t)(n > 0 ? n : 1));
@@ -401,6 +411,14 @@ void or_scaling(const OrProblem *p, double *out) { memcpy(out, p->scaling, sizeo
 
 /* y (+)= M x, M column-major r x c */
 static inline void matvec(const double *M, long r, long c, const double *x, double *y, int add) {
+    if (g_emu & OR_EMU_ACC) {
+        for (long i = 0; i < r; i++) {
+            float acc = add ? (float)y[i] : 0.f;
+            for (long k = 0; k < c; k++) acc = fmaf((float)M[k * r + i], (float)x[k], acc);
+            y[i] = acc;
+        }
+        return;
+    }
     if (!add) for (long i = 0; i < r; i++) y[i] = 0;
     for (long k = 0; k < c; k++) {
         const double xk = x[k];
@@ -411,11 +429,46 @@ static inline void matvec(const double *M, long r, long c, const double *x, doub
 
 /* y (+)= M' x, M column-major r x c, x length r, y length c */
 static inline void matTvec(const double *M, long r, long c, const double *x, double *y, int add) {
+    if (g_emu & OR_EMU_ACC) {
+        for (long k = 0; k < c; k++) {
+            float acc = 0.f;
+            for (long i = 0; i < r; i++) acc = fmaf((float)M[k * r + i], (float)x[i], acc);
+            y[k] = add ? (double)(float)(y[k] + acc) : acc;
+        }
+        return;
+    }
     for (long k = 0; k < c; k++) {
         const double *col = M + k * r;
         double acc = 0;
         for (long i = 0; i < r; i++) acc += col[i] * x[i];
         y[k] = add ? y[k] + acc : acc;
+    }
+}
+
+/* y = M x for the forward rollout: as matvec, or (OR_EMU_FWD64) accumulated in double, or
+ * (OR_EMU_FWDC) float with compensation -- Ogita, Rump & Oishi, "Accurate sum and dot
+ * product", SIAM J. Sci. Comput. 26 (2005), algorithm Dot2: each product split into its
+ * rounded value and exact error by an FMA, each sum by Knuth's TwoSum. */
+static void matvec_fwd(const double *M, long r, long c, const double *x, double *y) {
+    if (!(g_emu & OR_EMU_ACC) || !(g_emu & (OR_EMU_FWD64 | OR_EMU_FWDC))) { matvec(M, r, c, x, y, 0); return; }
+    if (g_emu & OR_EMU_FWD64) {
+        for (long i = 0; i < r; i++) {
+            double acc = 0;
+            for (long k = 0; k < c; k++) acc += M[k * r + i] * x[k];
+            y[i] = acc;
+        }
+        return;
+    }
+    for (long i = 0; i < r; i++) {
+        float s = 0.f, comp = 0.f;
+        for (long k = 0; k < c; k++) {
+            const float a = (float)M[k * r + i], b = (float)x[k];
+            const float pr = a * b, e = fmaf(a, b, -pr);
+            const float t = s + pr, bv = t - s;
+            comp += ((s - (t - bv)) + (pr - bv)) + e;
+            s = t;
+        }
+        y[i] = s + comp;
     }
 }
 
@@ -490,6 +543,7 @@ void or_op(const OrProblem *p, const double *prim, double *dual) {
             o[nx + 1] = h;
         }
     }
+    EMU_VEC(dual, p->sDual);
 }
 
 void or_adj(const OrProblem *p, const double *dual, double *prim) {
@@ -554,6 +608,7 @@ void or_adj(const OrProblem *p, const double *dual, double *prim) {
             s[nnl + jj] = 0.5 * d23;
         }
     }
+    EMU_VEC(prim, p->sPrim);
 }
 
 /* ------------------------------------------------------------------ proximal pieces */
@@ -592,6 +647,7 @@ void or_project_dynamics(const OrProblem *p, const double *x0, double *x, double
                 for (long k = 0; k < nu; k++) di[k] -= tmp[k];
             }
             chol_solve(p->chol + i * nu * nu, nu, di);
+            EMU_VEC(di, nu);
             if (stage > 0) {
                 double *qi = q + i * nx;
                 for (long k = 0; k < nx; k++) qi[k] = 0;
@@ -602,21 +658,25 @@ void or_project_dynamics(const OrProblem *p, const double *x0, double *x, double
                 for (long k = 0; k < nu; k++) tmp[k] = di[k] - u[i * nu + k];
                 matTvec(p->K + i * nu * nx, nu, nx, tmp, qi, 1); /* K' (d - u) */
                 for (long k = 0; k < nx; k++) qi[k] -= x[i * nx + k];
+                EMU_VEC(qi, nx);
             }
         }
     }
     for (long k = 0; k < nx; k++) x[k] = x0[k];
+    EMU_VEC(x, nx);
     for (long stage = 0; stage < p->ns - 1; stage++) {
         for (long i = p->stageFrom[stage]; i <= p->stageTo[stage]; i++) {
             double *ui = u + i * nu;
-            matvec(p->K + i * nu * nx, nu, nx, x + i * nx, ui, 0);
+            matvec_fwd(p->K + i * nu * nx, nu, nx, x + i * nx, ui);
             for (long k = 0; k < nu; k++) ui[k] += d[i * nu + k];
+            EMU_VEC(ui, nu);
             memcpy(tmp, x + i * nx, sizeof(double) * (size_t)nx);
             memcpy(tmp + nx, ui, sizeof(double) * (size_t)nu);
             for (long j = p->chFrom[i]; j < p->chFrom[i] + p->numCh[i]; j++) {
-                matvec(p->AB + j * nx * p->nxu, nx, p->nxu, tmp, x + j * nx, 0);
+                matvec_fwd(p->AB + j * nx * p->nxu, nx, p->nxu, tmp, x + j * nx);
                 if (p->affine)
                     for (long k = 0; k < nx; k++) x[j * nx + k] += p->e[j * nx + k];
+                EMU_VEC(x + j * nx, nx);
             }
         }
     }
@@ -634,6 +694,7 @@ void or_project_kernel(const OrProblem *p, double *y, double *t, double *s) {
         memcpy(v, y + i * yD, sizeof(double) * (size_t)yD);
         for (long k = 0; k < nc; k++) { v[yD + k] = t[c0 + k]; v[yD + E + k] = s[c0 + k]; }
         matvec(p->NNtr + i * nd * nd, nd, nd, v, w, 0);
+        EMU_VEC(w, nd);
         memcpy(y + i * yD, w, sizeof(double) * (size_t)yD);
         for (long k = 0; k < nc; k++) { t[c0 + k] = w[yD + k]; s[c0 + k] = w[yD + E + k]; }
     }
@@ -701,6 +762,7 @@ void or_project_dual(const OrProblem *p, double *dual) {
     if (p->sV) or_project_box(dual + p->oV, p->lLb, p->lUb, p->sV);
     if (p->costL == COST_LIN) project_linear_epi(dual + p->oVI, p->nl);
     else or_project_soc_columns(dual + p->oVI, p->nx + 2, p->nl);
+    EMU_VEC(dual, p->sDual);
 }
 
 /* One Chambolle-Pock step: cand = T(z) (cache.cuh:748-801). x0s is the scaled initial state. */
@@ -725,15 +787,19 @@ static void cp_step(const OrProblem *p, Work *w, const double *x0s, const double
     /* modifyPrimal: p - gamma L* d */
     or_adj(p, zd, w->pw);
     for (long i = 0; i < sp; i++) w->pw[i] = w->pw[i] * -g + zp[i];
+    EMU_VEC(w->pw, sp);
     /* proximalPrimal: s_root -= gamma; dynamics; kernels */
     w->pw[p->oS] -= g;
+    EMU_VEC(w->pw + p->oS, 1);
     or_project_dynamics(p, x0s, w->pw + p->oX, w->pw);
     or_project_kernel(p, w->pw + p->oY, w->pw + p->oT, w->pw + p->oS);
     memcpy(cp, w->pw, sizeof(double) * (size_t)sp);
     /* modifyDual: d + gamma L(2 pbar - p) */
     for (long i = 0; i < sp; i++) w->pd[i] = 2. * cp[i] - zp[i];
+    EMU_VEC(w->pd, sp);
     or_op(p, w->pd, w->dw);
     for (long i = 0; i < sd; i++) w->dw[i] = w->dw[i] * g + zd[i];
+    EMU_VEC(w->dw, sd);
     /* proximalDual (Moreau): cand = gamma (v - proj_C(v)), v = dbar/gamma + translation */
     for (long i = 0; i < sd; i++) w->dw[i] *= gi;
     if (p->costNl != COST_LIN)
@@ -741,9 +807,11 @@ static void cp_step(const OrProblem *p, Work *w, const double *x0s, const double
     if (p->costL != COST_LIN)
         for (long jj = 0; jj < p->nl; jj++)
             for (long k = 0; k < p->nx + 2; k++) w->dw[p->oVI + jj * (p->nx + 2) + k] += p->lTrans[k];
+    EMU_VEC(w->dw, sd);
     memcpy(cd, w->dw, sizeof(double) * (size_t)sd);
     or_project_dual(p, w->dw);
     for (long i = 0; i < sd; i++) cd[i] = (cd[i] - w->dw[i]) * g;
+    EMU_VEC(cd, sd);
 }
 
 void or_cp_step(const OrProblem *p, const double *x0s, const double *z, double *cand) {
@@ -759,6 +827,7 @@ static void apply_m(const OrProblem *p, const double *yv, double *my) {
     or_adj(p, yv + sp, my);
     or_op(p, yv, my + sp);
     for (long i = 0; i < p->sZ; i++) my[i] = yv[i] - p->step * my[i];
+    EMU_VEC(my, p->sZ);
 }
 
 double or_dot_m(const OrProblem *p, const double *x, const double *y) {
@@ -808,6 +877,56 @@ static void lstsq_qr(const double *A0, long n, long m, const double *b0, double 
     }
     free(A);
     free(b);
+}
+
+/* OR_EMU_GRAM: min ||A g - b|| by the normal equations, as a GPU controller with float data
+ * solves it -- Gram matrix and right-hand side accumulated with float FMAs over blocks of 256
+ * rows and summed in double, a ridge of 1e-7 x the largest diagonal entry, FP64 Cholesky.
+ * Returns 0 on breakdown (the caller then takes the plain residual direction). */
+static int gram_solve(const double *A, long n, long m, const double *b, double *g) {
+    double G[64], h[64], L[64], y[8];
+    if (m > 8) return 0;
+    for (long i = 0; i < m; i++)
+        for (long j = 0; j <= m; j++) {
+            if (j < m && j > i) continue;
+            const double *v = j < m ? A + j * n : b;
+            double s = 0;
+            for (long c = 0; c < n; c += 256) {
+                float acc = 0.f;
+                for (long k = c; k < c + 256 && k < n; k++) acc = fmaf((float)A[i * n + k], (float)v[k], acc);
+                s += acc;
+            }
+            if (j < m) G[i * m + j] = G[j * m + i] = s;
+            else h[i] = s;
+        }
+    double dmax = 0;
+    for (long i = 0; i < m; i++) dmax = fmax(dmax, G[i * m + i]);
+    if (!(dmax > 0)) return 0;
+    for (long j = 0; j < m; j++) {
+        double s = G[j * m + j] + 1e-7 * dmax;
+        for (long k = 0; k < j; k++) s -= L[j * m + k] * L[j * m + k];
+        if (!(s > 0)) return 0;
+        const double d = sqrt(s);
+        L[j * m + j] = d;
+        for (long i = j + 1; i < m; i++) {
+            double a = G[i * m + j];
+            for (long k = 0; k < j; k++) a -= L[i * m + k] * L[j * m + k];
+            L[i * m + j] = a / d;
+        }
+    }
+    for (long i = 0; i < m; i++) {
+        double a = h[i];
+        for (long k = 0; k < i; k++) a -= L[i * m + k] * y[k];
+        y[i] = a / L[i * m + i];
+    }
+    for (long i = m - 1; i >= 0; i--) {
+        double a = y[i];
+        for (long k = i + 1; k < m; k++) a -= L[k * m + i] * g[k];
+        g[i] = a / L[i * m + i];
+    }
+    for (long i = 0; i < m; i++)
+        if (!isfinite(g[i])) return 0;
+    return 1;
 }
 
 static double now_s(void) {
@@ -930,6 +1049,7 @@ int or_run_spock(const OrProblem *p, const OrOptions *o, const double *x0, doubl
         memset(z, 0, B);
         for (long i = 0; i < nz; i++) { prev[i] = 1.; rprev[i] = 1.; } /* cache.cuh:624-632 */
     } else {
+        EMU_VEC(z, nz);
         memcpy(prev, z, B);
         memset(rprev, 0, B);
     }
@@ -942,6 +1062,7 @@ int or_run_spock(const OrProblem *p, const OrOptions *o, const double *x0, doubl
         cp_step(p, &w, x0s, z, cand);
         calls++;
         for (long k = 0; k < nz; k++) r[k] = z[k] - cand[k];
+        EMU_VEC(r, nz);
         apply_m(p, r, mr);
         ctl_check(&c, iOut, mr, nz);
         if (c.status != -1) { memcpy(z, cand, B); break; }
@@ -955,9 +1076,14 @@ int or_run_spock(const OrProblem *p, const OrOptions *o, const double *x0, doubl
             memmove(andZ + nz, andZ, B * (size_t)(m - 1));
             memmove(andR + nz, andR, B * (size_t)(m - 1));
         }
+        EMU_VEC(dz, nz);
+        EMU_VEC(dr, nz);
         for (long k = 0; k < nz; k++) { andR[k] = dr[k]; andZ[k] = dz[k] - dr[k]; }
-        if (iOut >= m) {
-            lstsq_qr(andR, nz, m, r, gam);
+        EMU_VEC(andZ, nz);
+        int useAnd = iOut >= m;
+        if (useAnd && (g_emu & OR_EMU_GRAM)) useAnd = gram_solve(andR, nz, m, r, gam);
+        else if (useAnd) lstsq_qr(andR, nz, m, r, gam);
+        if (useAnd) {
             for (long k = 0; k < nz; k++) {
                 double acc = 0;
                 for (long j = 0; j < m; j++) acc += andZ[j * nz + k] * gam[j];
@@ -966,8 +1092,10 @@ int or_run_spock(const OrProblem *p, const OrOptions *o, const double *x0, doubl
         } else {
             for (long k = 0; k < nz; k++) dir[k] = -r[k];
         }
+        EMU_VEC(dir, nz);
         if (wv <= c0 * zeta) { /* K0: blind update */
             for (long k = 0; k < nz; k++) cand[k] = prev[k] + dir[k];
+            EMU_VEC(cand, nz);
             zeta = wv;
             k0++;
             continue;
@@ -975,9 +1103,12 @@ int or_run_spock(const OrProblem *p, const OrOptions *o, const double *x0, doubl
         tau = 1.;
         for (long iIn = 0; iIn < o->max_inner; iIn++) {
             for (long k = 0; k < nz; k++) { dsc[k] = dir[k] * tau; z[k] = prev[k] + dsc[k]; }
+            EMU_VEC(dsc, nz);
+            EMU_VEC(z, nz);
             cp_step(p, &w, x0s, z, cand);
             calls++;
             for (long k = 0; k < nz; k++) r[k] = z[k] - cand[k];
+            EMU_VEC(r, nz);
             apply_m(p, r, mr);
             wTilde = sqrt(dotv(r, mr, nz));
             if (wv <= wSafe && wTilde <= c1 * wv) { /* K1: educated update */
@@ -990,6 +1121,7 @@ int or_run_spock(const OrProblem *p, const OrOptions *o, const double *x0, doubl
             if (rho >= sigma * wTilde * wv) { /* K2: safeguard */
                 const double f = lambda * rho / (wTilde * wTilde);
                 for (long k = 0; k < nz; k++) cand[k] = prev[k] - r[k] * f;
+                EMU_VEC(cand, nz);
                 k2++;
                 break;
             } else {

@@ -90,6 +90,19 @@ void or_offline_kernel(const OrProblem *p, double alpha, long node, double *nntr
 /* Largest eigenvalue of L*L by power iteration (problem.py:402-417 computes it with ARPACK). */
 double or_norm_L_sq(const OrProblem *p, long iters);
 
+/* FP32 emulation (process-wide; 0 = plain FP64, the default).  Explains how single-precision
+ * arithmetic changes the iteration's path, without a GPU:
+ *   OR_EMU_DATA   problem data rounded to float when a problem is loaded (set before or_load);
+ *   OR_EMU_ACC    every small matrix-vector product accumulated with float FMAs;
+ *   OR_EMU_VEC    every vector of the CP step and of the SuperMann loop stored as float;
+ *   OR_EMU_GRAM   Anderson by normal equations: float-accumulated Gram matrix, ridge 1e-7 x its
+ *                 largest diagonal entry, FP64 Cholesky (instead of Householder QR);
+ *   OR_EMU_FWD64  the forward rollout of the dynamics projection accumulated in double;
+ *   OR_EMU_FWDC   the forward rollout accumulated in float with compensation (the Dot2
+ *                 algorithm: error-free products by FMA, TwoSum additions). */
+enum { OR_EMU_DATA = 1, OR_EMU_ACC = 2, OR_EMU_VEC = 4, OR_EMU_GRAM = 8, OR_EMU_FWD64 = 16, OR_EMU_FWDC = 32 };
+void or_set_emulation(int mode);
+
 #ifdef __cplusplus
 }
 #endif

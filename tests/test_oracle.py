@@ -189,3 +189,26 @@ def test_input_ball_projection(oracle_lib, tmp_problems):
         x1 = out[oIII + i * nxu:oIII + i * nxu + P.nx]
         if i > 0:
             assert (np.abs(x1) <= 3 + 1e-12).all()
+
+
+def test_fp32_emulation_modes(oracle_lib):
+    """The oracle's FP32 emulation (spock_oracle.h, OR_EMU_*): under the GPU-like mode a CP step
+    returns float-representable values within single-precision distance of the FP64 step; the
+    forward-rollout remedies keep that; switching back to mode 0 restores FP64 bit for bit."""
+    path = os.path.join(GOLDEN, "cfg1")
+    P = oracle_lib.Problem(path)
+    rng = np.random.default_rng(8)
+    z = rng.standard_normal(P.size)
+    x0s = rng.uniform(-1, 1, P.nx) * P.scaling[:P.nx]
+    a = P.cp_step(x0s, z)
+    try:
+        for mode in (oracle_lib.EMU_GPU_FP32, oracle_lib.EMU_GPU_FP32 | oracle_lib.EMU_FWD64,
+                     oracle_lib.EMU_GPU_FP32 | oracle_lib.EMU_FWDC):
+            oracle_lib.set_emulation(mode)
+            b = oracle_lib.Problem(path).cp_step(x0s.astype(np.float32).astype(np.float64),
+                                                 z.astype(np.float32).astype(np.float64))
+            assert np.array_equal(b, b.astype(np.float32).astype(np.float64))
+            assert 0 < np.abs(b - a).max() <= 1e-4 * np.abs(a).max()
+    finally:
+        oracle_lib.set_emulation(0)
+    assert np.array_equal(P.cp_step(x0s, z), a)
