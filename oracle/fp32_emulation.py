@@ -30,6 +30,7 @@ MODES = {
     "gpu_fp32": O.EMU_GPU_FP32,
     "gpu_fp32_fwd64": O.EMU_GPU_FP32 | O.EMU_FWD64,
     "gpu_fp32_fwd_dot2": O.EMU_GPU_FP32 | O.EMU_FWDC,
+    "gpu_fp32_fwd_dot2_states": O.EMU_GPU_FP32 | O.EMU_FWDCX,
 }
 
 

@@ -445,12 +445,13 @@ static inline void matTvec(const double *M, long r, long c, const double *x, dou
     }
 }
 
-/* y = M x for the forward rollout: as matvec, or (OR_EMU_FWD64) accumulated in double, or
- * (OR_EMU_FWDC) float with compensation -- Ogita, Rump & Oishi, "Accurate sum and dot
+/* y = M x for the forward rollout (`states` = 1 for [A B][x; u], 0 for K x): as matvec, or
+ * (OR_EMU_FWD64) accumulated in double, or (OR_EMU_FWDC, OR_EMU_FWDCX) float with compensation -- Ogita, Rump & Oishi, "Accurate sum and dot
  * product", SIAM J. Sci. Comput. 26 (2005), algorithm Dot2: each product split into its
  * rounded value and exact error by an FMA, each sum by Knuth's TwoSum. */
-static void matvec_fwd(const double *M, long r, long c, const double *x, double *y) {
-    if (!(g_emu & OR_EMU_ACC) || !(g_emu & (OR_EMU_FWD64 | OR_EMU_FWDC))) { matvec(M, r, c, x, y, 0); return; }
+static void matvec_fwd(const double *M, long r, long c, const double *x, double *y, int states) {
+    const int comp = (g_emu & OR_EMU_FWDC) || ((g_emu & OR_EMU_FWDCX) && states);
+    if (!(g_emu & OR_EMU_ACC) || !((g_emu & OR_EMU_FWD64) || comp)) { matvec(M, r, c, x, y, 0); return; }
     if (g_emu & OR_EMU_FWD64) {
         for (long i = 0; i < r; i++) {
             double acc = 0;
@@ -667,13 +668,13 @@ void or_project_dynamics(const OrProblem *p, const double *x0, double *x, double
     for (long stage = 0; stage < p->ns - 1; stage++) {
         for (long i = p->stageFrom[stage]; i <= p->stageTo[stage]; i++) {
             double *ui = u + i * nu;
-            matvec_fwd(p->K + i * nu * nx, nu, nx, x + i * nx, ui);
+            matvec_fwd(p->K + i * nu * nx, nu, nx, x + i * nx, ui, 0);
             for (long k = 0; k < nu; k++) ui[k] += d[i * nu + k];
             EMU_VEC(ui, nu);
             memcpy(tmp, x + i * nx, sizeof(double) * (size_t)nx);
             memcpy(tmp + nx, ui, sizeof(double) * (size_t)nu);
             for (long j = p->chFrom[i]; j < p->chFrom[i] + p->numCh[i]; j++) {
-                matvec_fwd(p->AB + j * nx * p->nxu, nx, p->nxu, tmp, x + j * nx);
+                matvec_fwd(p->AB + j * nx * p->nxu, nx, p->nxu, tmp, x + j * nx, 1);
                 if (p->affine)
                     for (long k = 0; k < nx; k++) x[j * nx + k] += p->e[j * nx + k];
                 EMU_VEC(x + j * nx, nx);

@@ -99,8 +99,10 @@ double or_norm_L_sq(const OrProblem *p, long iters);
  *                 largest diagonal entry, FP64 Cholesky (instead of Householder QR);
  *   OR_EMU_FWD64  the forward rollout of the dynamics projection accumulated in double;
  *   OR_EMU_FWDC   the forward rollout accumulated in float with compensation (the Dot2
- *                 algorithm: error-free products by FMA, TwoSum additions). */
-enum { OR_EMU_DATA = 1, OR_EMU_ACC = 2, OR_EMU_VEC = 4, OR_EMU_GRAM = 8, OR_EMU_FWD64 = 16, OR_EMU_FWDC = 32 };
+ *                 algorithm: error-free products by FMA, TwoSum additions);
+ *   OR_EMU_FWDCX  the same for the children's states [A B][x; u] only (u = Kx + d plain). */
+enum { OR_EMU_DATA = 1, OR_EMU_ACC = 2, OR_EMU_VEC = 4, OR_EMU_GRAM = 8, OR_EMU_FWD64 = 16, OR_EMU_FWDC = 32,
+       OR_EMU_FWDCX = 64 };
 void or_set_emulation(int mode);
 
 #ifdef __cplusplus
