@@ -14,6 +14,10 @@ Sizes:
   config3: i.i.d. process with 5 equiprobable events, N=8, tau=3 -> 781 nodes; nx=100, nu=40;
            dynamics generated as config2; quadratic costs; box |x|<=3 and the input ball
            ||u||_2 <= 2 (RectangleInputBall); AVaR(0.9).
+  config4 uniform: config2 with `count` initial states (one problem, a batch of instances).
+  config4 mixed (config4_mixed): `count` problems, each from its own seed, built like config2
+           with nx ~ U{8..96}, nu = nx // 2, a Markov chain of 2-4 states, N ~ U{5..15},
+           tau ~ U{2..4} (tau < N), costs x `cost_scale`; one initial state each.
 """
 import os
 
@@ -96,6 +100,28 @@ def config3(path, seed=0, count=1, nx=100, nu=40, horizon=8, stopping=3, events=
      .with_preconditioning(False)
      .generate_problem(path))
     return path, rng.uniform(-1., 1., size=(count, nx))
+
+
+def config4_mixed(root, seed=0, count=256, nx_range=(8, 96), states_range=(2, 4), horizon_range=(5, 15),
+                  stopping_range=(2, 4), cost_scale=1e-3):
+    """Write `count` problems under root/config4_mixed_s{seed}/p{k}/ (each kept if already there);
+    returns [(path, x0)] with one initial state (nx,) per problem.  The ranges are inclusive."""
+    import json
+    out = []
+    for k in range(count):
+        rng = np.random.default_rng([seed, k])
+        nx = int(rng.integers(nx_range[0], nx_range[1] + 1))
+        states = int(rng.integers(states_range[0], states_range[1] + 1))
+        horizon = int(rng.integers(horizon_range[0], horizon_range[1] + 1))
+        stopping = int(min(rng.integers(stopping_range[0], stopping_range[1] + 1), horizon - 1))
+        sub = int(rng.integers(0, 2 ** 31))
+        path = os.path.join(root, f"config4_mixed_s{seed}", f"p{k:04d}", "")
+        if not os.path.exists(os.path.join(path, "data.json")):
+            config2(path, seed=sub, nx=nx, nu=max(1, nx // 2), horizon=horizon, stopping=stopping, states=states,
+                    cost_scale=cost_scale)
+        assert json.load(open(os.path.join(path, "data.json")))["numStates"] == nx
+        out.append((path, rng.uniform(-1., 1., size=nx)))
+    return out
 
 
 BUILDERS = {"config1": config1, "config2": config2, "config3": config3}

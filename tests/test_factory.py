@@ -171,3 +171,25 @@ def test_polyhedron_with_identity(oracle_lib, tmp_path, preconditioning):
     off = prob.y_dim * nnl + nnl                  # after the risk rows and s - b'y
     assert d[off + (nx + nu) * 1 + 0] == 1.
     assert np.count_nonzero(d[off:off + (nx + nu) * nnl]) == 1
+
+
+def test_config4_mixed(oracle_lib, tmp_path):
+    """The mixed batch of config 4: each problem has its own seed and sizes drawn from the given
+    ranges, is kept on disk once written, and solves (FP64 oracle, tol 1e-3)."""
+    from spock_gb300 import configs
+    kw = dict(count=4, nx_range=(3, 6), states_range=(2, 3), horizon_range=(3, 5), stopping_range=(2, 3))
+    probs = configs.config4_mixed(str(tmp_path), seed=1, **kw)
+    assert len(probs) == 4 and len({p for p, _ in probs}) == 4
+    sizes = set()
+    for path, x0 in probs:
+        meta = json.load(open(path + "data.json"))
+        nx, nu = meta["numStates"], meta["numInputs"]
+        assert 3 <= nx <= 6 and nu == nx // 2 and x0.shape == (nx,)
+        assert 2 <= meta["numEvents"] <= 3 and 4 <= meta["numStages"] <= 6
+        sizes.add((nx, meta["numNodes"]))
+        P = oracle_lib.Problem(path)
+        z, st = P.run(x0, oracle_lib.options(tol=1e-3, anderson=5, max_iters=20000), "spock")
+        assert st.status == 0
+    assert len(sizes) > 1
+    again = configs.config4_mixed(str(tmp_path), seed=1, **kw)
+    assert all(a[0] == b[0] and np.array_equal(a[1], b[1]) for a, b in zip(probs, again))
