@@ -31,6 +31,7 @@ MODES = {
     "gpu_fp32_fwd64": O.EMU_GPU_FP32 | O.EMU_FWD64,
     "gpu_fp32_fwd_dot2": O.EMU_GPU_FP32 | O.EMU_FWDC,
     "gpu_fp32_fwd_dot2_states": O.EMU_GPU_FP32 | O.EMU_FWDCX,
+    "gpu_fp32_fwd_kahan": O.EMU_GPU_FP32 | O.EMU_FWDK,
 }
 
 

@@ -85,7 +85,7 @@ def lib():
 
 # FP32 emulation modes (spock_oracle.h): problem data, matvec accumulation, vector storage,
 # Anderson normal equations, and the two remedies for the forward rollout.
-EMU_DATA, EMU_ACC, EMU_VEC, EMU_GRAM, EMU_FWD64, EMU_FWDC, EMU_FWDCX = 1, 2, 4, 8, 16, 32, 64
+EMU_DATA, EMU_ACC, EMU_VEC, EMU_GRAM, EMU_FWD64, EMU_FWDC, EMU_FWDCX, EMU_FWDK = 1, 2, 4, 8, 16, 32, 64, 128
 EMU_GPU_FP32 = EMU_DATA | EMU_ACC | EMU_VEC | EMU_GRAM
 
 

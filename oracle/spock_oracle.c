@@ -451,12 +451,26 @@ static inline void matTvec(const double *M, long r, long c, const double *x, dou
  * rounded value and exact error by an FMA, each sum by Knuth's TwoSum. */
 static void matvec_fwd(const double *M, long r, long c, const double *x, double *y, int states) {
     const int comp = (g_emu & OR_EMU_FWDC) || ((g_emu & OR_EMU_FWDCX) && states);
-    if (!(g_emu & OR_EMU_ACC) || !((g_emu & OR_EMU_FWD64) || comp)) { matvec(M, r, c, x, y, 0); return; }
+    const int kahan = (g_emu & OR_EMU_FWDK) != 0;
+    if (!(g_emu & OR_EMU_ACC) || !((g_emu & OR_EMU_FWD64) || comp || kahan)) { matvec(M, r, c, x, y, 0); return; }
     if (g_emu & OR_EMU_FWD64) {
         for (long i = 0; i < r; i++) {
             double acc = 0;
             for (long k = 0; k < c; k++) acc += M[k * r + i] * x[k];
             y[i] = acc;
+        }
+        return;
+    }
+    if (kahan && !comp) { /* Kahan: s += a*b (rounded) with a running correction */
+        for (long i = 0; i < r; i++) {
+            float s = 0.f, cr = 0.f;
+            for (long k = 0; k < c; k++) {
+                const float yv = (float)M[k * r + i] * (float)x[k] - cr;
+                const float t = s + yv;
+                cr = (t - s) - yv;
+                s = t;
+            }
+            y[i] = s;
         }
         return;
     }

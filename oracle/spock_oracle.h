@@ -100,9 +100,11 @@ double or_norm_L_sq(const OrProblem *p, long iters);
  *   OR_EMU_FWD64  the forward rollout of the dynamics projection accumulated in double;
  *   OR_EMU_FWDC   the forward rollout accumulated in float with compensation (the Dot2
  *                 algorithm: error-free products by FMA, TwoSum additions);
- *   OR_EMU_FWDCX  the same for the children's states [A B][x; u] only (u = Kx + d plain). */
+ *   OR_EMU_FWDCX  the same for the children's states [A B][x; u] only (u = Kx + d plain);
+ *   OR_EMU_FWDK   the forward rollout with Kahan's compensated summation of the rounded float
+ *                 products (half the operations of Dot2; the products' own errors remain). */
 enum { OR_EMU_DATA = 1, OR_EMU_ACC = 2, OR_EMU_VEC = 4, OR_EMU_GRAM = 8, OR_EMU_FWD64 = 16, OR_EMU_FWDC = 32,
-       OR_EMU_FWDCX = 64 };
+       OR_EMU_FWDCX = 64, OR_EMU_FWDK = 128 };
 void or_set_emulation(int mode);
 
 #ifdef __cplusplus

@@ -203,7 +203,8 @@ def test_fp32_emulation_modes(oracle_lib):
     a = P.cp_step(x0s, z)
     try:
         for mode in (oracle_lib.EMU_GPU_FP32, oracle_lib.EMU_GPU_FP32 | oracle_lib.EMU_FWD64,
-                     oracle_lib.EMU_GPU_FP32 | oracle_lib.EMU_FWDC, oracle_lib.EMU_GPU_FP32 | oracle_lib.EMU_FWDCX):
+                     oracle_lib.EMU_GPU_FP32 | oracle_lib.EMU_FWDC, oracle_lib.EMU_GPU_FP32 | oracle_lib.EMU_FWDCX,
+                     oracle_lib.EMU_GPU_FP32 | oracle_lib.EMU_FWDK):
             oracle_lib.set_emulation(mode)
             b = oracle_lib.Problem(path).cp_step(x0s.astype(np.float32).astype(np.float64),
                                                  z.astype(np.float32).astype(np.float64))
