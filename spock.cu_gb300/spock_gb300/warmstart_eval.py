@@ -4,10 +4,10 @@
 
 (run from spock.cu_gb300/, or with it on sys.path).  Training data: cold FP32 batch solves of
 `--train` initial states x0 ~ U[-1, 1]^50 of config 2 with costs x 1e-3 (the benchmark problem)
-at tol(--train-tol); config 5 names 200k solves at 1e-5, which the FP32 iteration does not reach
-in reasonable time (the float accumulation of its forward dynamics rollout leaves ~1e-6 noise in
-T(z), and Anderson steps fail near that level).  Model: PCA(128) of the solutions + MLP 50 -> 1024
--> 1024 -> 128 (GELU, BF16
+at tol(--train-tol); config 5 names 200k solves at 1e-5, which this problem's iteration does not
+reach in reasonable time (the FP64 oracle converges for 2 of 8 cold starts within 4,000 outer
+iterations; FP32 also suffers from the float accumulation of its forward dynamics rollout).
+Model: PCA(128) of the solutions + MLP 50 -> 1024 -> 1024 -> 128 (GELU, BF16
 weights, FP32 accumulation), trained with the library's kernels.  Evaluation: `--test` held-out
 x0 in one batch, solved to tol(1e-4) in FP32 (i) cold, (ii) cold to the absolute tolerance only
 (the tolerance a warm start meets), (iii) from the MLP's predicted iterate and (iv) from the
