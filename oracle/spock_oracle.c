@@ -15,6 +15,8 @@
  *     (cache.cuh:909-961), Anderson direction (cache.cuh:860-904) and the SuperMann / CP loops
  *     (cache.cuh:966-1132);
  *   - the offline cache (problem.py:192-231) and step size (problem.py:402-417).
+ * On request it also emulates single precision (or_set_emulation, spock_oracle.h), to explain
+ * the iteration counts of the FP32 GPU path; mode 0, the default, is the plain FP64 restatement.
  */
 #include "spock_oracle.h"
 
