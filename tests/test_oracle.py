@@ -213,3 +213,31 @@ def test_fp32_emulation_modes(oracle_lib):
     finally:
         oracle_lib.set_emulation(0)
     assert np.array_equal(P.cp_step(x0s, z), a)
+
+
+def test_fp32_emulation_forward_rollout(oracle_lib, tmp_problems):
+    """On a config-2 sized problem (607 nodes, nx=50), the dynamics projection's deviation from
+    FP64 arithmetic on the same float data: float accumulation everywhere gives the largest; a
+    forward rollout accumulated in double or with Dot2 compensation cuts it; plain float storage
+    alone is smallest."""
+    from spock_gb300 import configs
+    path, x0 = configs.cached("config2", tmp_problems, seed=0, count=1, cost_scale=1e-3)
+    rng = np.random.default_rng(0)
+    P0 = oracle_lib.Problem(path)
+    x = rng.standard_normal(P0.nx * P0.n)
+    u = rng.standard_normal(P0.nu * P0.nnl)
+    x0s = (x0[0] * P0.scaling[:P0.nx]).astype(np.float32).astype(np.float64)
+    D, A, V = oracle_lib.EMU_DATA, oracle_lib.EMU_ACC, oracle_lib.EMU_VEC
+    err = {}
+    try:
+        oracle_lib.set_emulation(D)
+        ref = np.concatenate(oracle_lib.Problem(path).project_dynamics(x0s, x, u))
+        for name, mode in [("acc", D | A | V), ("fwd64", D | A | V | oracle_lib.EMU_FWD64),
+                           ("dot2", D | A | V | oracle_lib.EMU_FWDC), ("vec", D | V)]:
+            oracle_lib.set_emulation(mode)
+            out = np.concatenate(oracle_lib.Problem(path).project_dynamics(x0s, x, u))
+            err[name] = np.abs(out - ref).max() / np.abs(ref).max()
+    finally:
+        oracle_lib.set_emulation(0)
+    assert err["vec"] < err["dot2"] < err["acc"] and err["fwd64"] < err["acc"]
+    assert err["acc"] < 1e-5 and err["dot2"] < 0.6 * err["acc"]
