@@ -49,8 +49,6 @@ def parse():
     ap.add_argument("--max-iters", type=int, default=20000)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-fp64-baseline", action="store_true", help="skip the plain FP64 SPOCK solves on the GPU")
-    ap.add_argument("--measure", action="store_true",
-                    help="with --impl reference: full FP64 oracle re-solves, printing T evaluations per re-solve")
     return ap.parse_args()
 
 
@@ -146,91 +144,63 @@ class Clocks:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_sample(path, x0s, threads, iters):
-    """The oracle (FP64 C restatement of the reference iteration) on `threads` threads, one instance
-    each, stopped after `iters` outer SPOCK iterations.  Returns (seconds per T evaluation, wall
-    seconds): a T evaluation -- one CP step plus one M application -- is the unit of work every
-    SuperMann iteration spends one or more of."""
+def cpu_resolves(path, x0_steps, z_start, threads, max_iters):
+    """FP64 oracle re-solves on `threads` host threads, one instance each: instance i starts from
+    z_start[i] and is re-solved along x0_steps[k][i] (each re-solve warm-started from the last).
+    z_start (C-contiguous float64, count x size) is updated in place to the last solutions.
+    Returns (wall seconds per step, statuses, mean T evaluations) over the steps."""
     from oracle import oracle
     oracle.build()
     P = oracle.Problem(path)
-    opts = oracle.options(tol=TOL, anderson=ANDERSON, max_iters=iters)
-    x = np.ascontiguousarray(np.resize(x0s, (threads, P.nx)))
-    zs = np.zeros((threads, P.size))
-    secs, status, its, calls, _ = P.solve_many_warm(x, zs, opts, threads, warm=False)
-    return secs * threads / float(np.sum(calls)), secs
+    opts = oracle.options(tol=TOL, anderson=ANDERSON, max_iters=max_iters)
+    zs = z_start
+    secs, sts, calls = [], [], []
+    for x in x0_steps:
+        t, st, its, c, _ = P.solve_many_warm(x, zs, opts, threads, warm=True)
+        secs.append(t)
+        sts.append(st)
+        calls.append(c)
+    if not secs:
+        return secs, np.zeros(0, dtype=np.int32), 0.
+    return secs, np.concatenate(sts), float(np.mean(np.concatenate(calls)))
 
 
-def committed_cpu_calls():
-    """T evaluations per warm re-solve measured by full FP64 oracle re-solves of this workload
-    (profiles/cpu_oracle_config2.md, written by `python bench.py --impl reference --measure`)."""
-    fn = os.path.join(ROOT, "profiles", "cpu_oracle_config2.md")
-    if os.path.exists(fn):
-        for line in open(fn):
-            if line.startswith("mean_T_evaluations_per_resolve:"):
-                return float(line.split(":")[1])
-    return None
-
-
-def measure_cpu_resolves(args):
-    """Full FP64 oracle re-solves of `threads` instances along the benchmark's x0 trajectory:
-    cold solve, then warm re-solves; prints the mean T evaluations and iterations per re-solve."""
+def cpu_cold(path, x0s, threads, max_iters):
+    """FP64 oracle cold solves (one instance per thread); returns the solutions (count x size)."""
     from oracle import oracle
     oracle.build()
-    threads = os.cpu_count() or 1
-    path, x0s = workload(args.seed, args.batch)
     P = oracle.Problem(path)
-    n = min(threads, args.batch)
-    opts = oracle.options(tol=TOL, anderson=ANDERSON, max_iters=args.max_iters)
-    zs = np.zeros((n, P.size))
-    secs, st, its, calls, _ = P.solve_many_warm(x0s[:n], zs, opts, n, warm=False)
-    print(f"cold: {secs:.1f} s, converged {int((st == 0).sum())}/{n}, mean iterations {its.mean():.0f}, "
-          f"mean T evaluations {calls.mean():.0f}", flush=True)
-    rec_calls, rec_its = [], []
-    for k, x in enumerate(trajectory(x0s, args.warmup + args.steps, args.seed)):
-        secs, st, its, calls, _ = P.solve_many_warm(x[:n], zs, opts, n, warm=True)
-        print(f"re-solve {k}: {secs:.1f} s, converged {int((st == 0).sum())}/{n}, mean iterations {its.mean():.0f}, "
-              f"mean T evaluations {calls.mean():.0f}", flush=True)
-        if k >= args.warmup:
-            rec_calls.append(calls.mean())
-            rec_its.append(its.mean())
-    print(f"mean_T_evaluations_per_resolve: {np.mean(rec_calls):.1f}")
-    print(f"mean_outer_iterations_per_resolve: {np.mean(rec_its):.1f}")
-    print(f"instances: {n}, threads: {n}")
+    opts = oracle.options(tol=TOL, anderson=ANDERSON, max_iters=max_iters)
+    zs = np.zeros((x0s.shape[0], P.size))
+    P.solve_many_warm(x0s, zs, opts, threads, warm=False)
+    return zs
 
 
 def run_reference(args):
+    """The CPU implementation of the same iteration (the oracle's FP64 C restatement of the
+    reference solver), timed on every host thread: one instance per thread, solved cold (not
+    timed), then W warm-up and K timed receding-horizon re-solves along the benchmark's x0
+    trajectory, each warm-started from the instance's previous solution."""
     rank, world, _ = dist_info()
     if rank != 0:
         return
-    if args.measure:
-        measure_cpu_resolves(args)
-        return
     threads = os.cpu_count() or 1
-    path, x0s = workload(args.seed, max(threads, 1))
-    iters = 25
-    for _ in range(args.warmup):
-        cpu_sample(path, x0s, threads, iters)
-    per_call, t_total = [], 0.
-    for _ in range(args.steps):
-        spc, secs = cpu_sample(path, x0s, threads, iters)
-        per_call.append(spc)
-        t_total += secs
-    spc = statistics.median(per_call)
-    calls = committed_cpu_calls()
-    if calls is None:
-        print(json.dumps({"impl": "reference", "unavailable": "profiles/cpu_oracle_config2.md (T evaluations per "
-                                                               "re-solve) is missing"}))
-        return
-    value = threads / (spc * calls)
-    sample = (f"{threads} instances on {threads} threads, {iters} outer SPOCK iterations each per step (FP64 C "
-              f"oracle); solves/s = threads / (s per T evaluation x {calls:.0f} T evaluations per warm re-solve, "
-              f"measured by full FP64 oracle re-solves of this workload)")
+    n = min(threads, args.batch)
+    path, x0s = workload(args.seed, args.batch)
+    traj = [x[:n] for x in trajectory(x0s, args.warmup + args.steps, args.seed)]
+    zs = cpu_cold(path, x0s[:n], n, args.max_iters)
+    cpu_resolves(path, traj[:args.warmup], zs, n, args.max_iters)
+    secs, st, calls = cpu_resolves(path, traj[args.warmup:], zs, n, args.max_iters)
+    total = float(np.sum(secs))
+    value = n * args.steps / total
+    sample = (f"{n} instances on {n} threads (one each), FP64 C oracle; per step every instance is re-solved to "
+              f"tol(1e-4) warm-started from its previous solution; {int((st == 0).sum())}/{st.size} converged, "
+              f"{calls:.0f} T evaluations per re-solve")
     out = {"metric": METRIC, "value": value, "unit": "solves/s", "impl": "reference", "n_gpus": args.gpus,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / max(args.steps, 1),
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / max(args.steps, 1),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded)", "config": config_dict(args.batch, world),
-           "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port", "sample": sample},
+           "cpu_baseline": {"value": value, "unit": "solves/s", "cores": n, "kind": "port", "sample": sample},
            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
@@ -252,7 +222,27 @@ def fp64_cold_gpu(path, x0s, device, count, max_iters):
         its.append(c.solveIter())
     el = time.perf_counter() - t0
     return {"value": count / el, "unit": "solves/s", "solves": count, "converged": int(sum(s == 0 for s in st)),
-            "outer_iterations_mean": float(np.mean(its)), "seconds": el}
+            "outer_iterations_mean": float(np.mean(its)), "seconds": el,
+            "note": "cold FP64 solves stop at tol(1e-4)'s relative tolerance (about 1e-3 here)"}
+
+
+# DRAM bytes (read + write) of one launch of a kernel, from an ncu capture (dram__bytes_read.sum +
+# dram__bytes_write.sum) of this workload: {(kernel, batch): bytes}.  The bench reports it as
+# roofline.traffic when the dominant kernel and batch have an entry.
+TRAFFIC_BYTES = {}
+
+
+def fp64_error(z_gpu, z_ref, nu, scaling_u, size_prim, nodes):
+    """Error of the GPU's FP32 solutions against the FP64 oracle's solutions of the same instances
+    (same x0, same warm start, same tolerance): relative error of the optimal cost s_0 (the root's
+    s, the first entry of the primal s block) and max error of the unscaled first inputs u_0."""
+    oS = size_prim - nodes
+    cost_g, cost_r = z_gpu[:, oS], z_ref[:, oS]
+    u_g, u_r = z_gpu[:, :nu] / scaling_u, z_ref[:, :nu] / scaling_u
+    return {"cost_rel_err_max": float(np.max(np.abs(cost_g - cost_r) / np.maximum(np.abs(cost_r), 1e-30))),
+            "cost_rel_err_mean": float(np.mean(np.abs(cost_g - cost_r) / np.maximum(np.abs(cost_r), 1e-30))),
+            "u0_abs_err_max": float(np.max(np.abs(u_g - u_r))),
+            "u0_rel_err_max": float(np.max(np.abs(u_g - u_r)) / max(np.max(np.abs(u_r)), 1e-30))}
 
 
 def run_gpu(args):
@@ -268,11 +258,18 @@ def run_gpu(args):
     path, x0s = workload(args.seed, B, rank)
     tree = sg.ScenarioTree(path)
     data = sg.ProblemData(tree)
-    cache = (sg.CacheBuilder(tree, data).tol(TOL).andersonBuffer(ANDERSON).maxIters(args.max_iters)
-             .precision(32).batch(B).device(local).build())
+
+    def fp32_cache():
+        return (sg.CacheBuilder(tree, data).tol(TOL).andersonBuffer(ANDERSON).maxIters(args.max_iters)
+                .precision(32).batch(B).device(local).build())
+    cache = fp32_cache()
+    snap = fp32_cache()  # holds the iterate the timed steps start from, for the end-to-end replay
     nx, nu = tree.numStates(), tree.numInputs()
-    traj = trajectory(x0s, args.warmup + 2 * args.steps, args.seed, rank)
+    extra = 2  # untimed steps after the timed ones: GPU against the FP64 oracle on the same re-solves
+    traj = trajectory(x0s, args.warmup + args.steps + extra, args.seed, rank)
     x_dev = [torch.tensor(x.T.copy(), dtype=torch.float32, device=f"cuda:{local}").contiguous() for x in traj]
+    threads = os.cpu_count() or 1
+    sample = np.linspace(0, B - 1, min(threads, B)).astype(int)  # instances the CPU legs re-solve
 
     def barrier():
         if world > 1:
@@ -284,6 +281,7 @@ def run_gpu(args):
     cold_conv = int((cache.statuses() == 0).sum())
     for k in range(args.warmup):
         cache.resolveDevice(x_dev[k].data_ptr())
+    snap.copyIterateFrom(cache)
     clocks = Clocks(local)
     barrier()
     clocks.start()
@@ -309,16 +307,37 @@ def run_gpu(args):
     conv = st_all == 0
     value = B * world * args.steps / t_dev
 
-    # end to end through the public API: host x0 in (double), statuses + first inputs out
+    # end to end through the public API on the same steps: the iterate the timed steps started
+    # from is put back (not timed), then every step copies host x0 in (double) and reads the
+    # statuses, iterations and first inputs back
+    cache.copyIterateFrom(snap)
     barrier()
     t1 = time.perf_counter()
+    st_e2e = []
     for k in range(args.steps):
-        cache.resolveBatch(traj[args.warmup + args.steps + k])
+        st_e2e.append(cache.resolveBatch(traj[args.warmup + k]))
         u0 = cache.firstInputs()
     barrier()
-    t_e2e = time.perf_counter() - t1
+    t_e2e = max_over_ranks(time.perf_counter() - t1, world)
     e2e = {"value": B * world * args.steps / t_e2e, "unit": "solves/s",
-           "h2d_bytes_per_step": int(B * nx * 8), "d2h_bytes_per_step": int(B * (nu * 8 + 4 + 8))}
+           "h2d_bytes_per_step": int(B * nx * 8), "d2h_bytes_per_step": int(B * (nu * 8 + 4 + 8)),
+           "same_steps_as_value": True, "converged": int((np.concatenate(st_e2e) == 0).sum())}
+    del snap
+
+    # the same re-solves on the GPU (FP32) and in the FP64 oracle on the host cores: `extra` more
+    # steps, each instance of the sample starting from the GPU's solution of the step before
+    z_gpu, z_cpu, cpu_secs, cpu_st, cpu_calls = [], [], [], [], []
+    for k in range(extra):
+        x_next = traj[args.warmup + args.steps + k]
+        z_before = np.stack([cache.solution(int(b)) for b in sample]) if rank == 0 else None
+        cache.resolveBatch(x_next)
+        if rank == 0:
+            z_gpu.append(np.stack([cache.solution(int(b)) for b in sample]))
+            secs, cst, ccalls = cpu_resolves(path, [x_next[sample]], z_before, len(sample), args.max_iters)
+            z_cpu.append(z_before)  # updated in place to the oracle's solutions
+            cpu_secs += secs
+            cpu_st.append(cst)
+            cpu_calls.append(ccalls)
 
     # roofline of the dominant kernel: CUDA-event time of single launches on the solver stream
     per_kernel = {}
@@ -331,23 +350,23 @@ def run_gpu(args):
     except (OSError, KeyError, ValueError):
         peak, peak_src = 6800., "fallback"
     achieved = kbytes / (kms / 1e3) / 1e9
-    traffic = None
-    fn = os.path.join(ROOT, "profiles", "traffic.md")
-    if os.path.exists(fn):
-        for line in open(fn):
-            if line.startswith(f"{dom}_bytes_per_launch_b{B}:"):
-                traffic = float(line.split(":")[1])
+    traffic = TRAFFIC_BYTES.get((dom, B))
 
     out = None
     if rank == 0:
-        threads = os.cpu_count() or 1
-        spc, _ = cpu_sample(path, x0s, threads, 25)
-        mean_calls = float(np.mean(calls_all))
-        cpu_val = threads / (spc * mean_calls)
-        cpu = {"value": cpu_val, "unit": "solves/s", "cores": threads, "kind": "port",
-               "sample": f"{threads} instances x 25 outer SPOCK iterations (FP64 C oracle, {threads} threads) -> s per "
-                         f"T evaluation, times the {mean_calls:.0f} T evaluations per re-solve of this run"}
-        fp64 = None if args.no_fp64_baseline else fp64_cold_gpu(path, x0s, local, 2, args.max_iters)
+        # CPU baseline: the FP64 oracle's re-solves of the sample above, one instance per thread
+        n = len(sample)
+        cst = np.concatenate(cpu_st)
+        cpu = {"value": n * len(cpu_secs) / float(np.sum(cpu_secs)), "unit": "solves/s", "cores": n, "kind": "port",
+               "sample": f"{n} instances x {len(cpu_secs)} warm re-solves of this workload (each from the GPU's "
+                         f"solution of the step before), FP64 C oracle, one instance per thread; "
+                         f"{int((cst == 0).sum())}/{cst.size} converged, {np.mean(cpu_calls):.0f} T evaluations "
+                         f"per re-solve"}
+        err = fp64_error(np.concatenate(z_gpu), np.concatenate(z_cpu), nu, data.scaling()[nx:nx + nu],
+                         cache.sizePrimal(), tree.numNodes())
+        err.update({"instances": int(cst.size), "reference": "FP64 oracle (CPU): same x0, same warm start, same "
+                    "tol(1e-4)", "reference_converged": int((cst == 0).sum())})
+        fp64 = None if args.no_fp64_baseline else fp64_cold_gpu(path, x0s, local, 16, args.max_iters)
         out = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
@@ -357,7 +376,7 @@ def run_gpu(args):
                             "kernel_ms": kms, "algorithmic_bytes": kbytes,
                             "per_kernel_ms": {k: v[0] for k, v in per_kernel.items()},
                             "per_kernel_gbs": {k: v[1] / v[0] / 1e6 for k, v in per_kernel.items()}},
-               "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
+               "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches), "fp64_error": err,
                "converged": int(conv.sum()), "instances": int(st_all.size), "cold_start_converged": cold_conv,
                "outer_iterations": {"mean": float(np.mean(it_all)), "max": int(np.max(it_all))},
                "t_evaluations_mean": float(np.mean(calls_all)), "rounds_per_step": rounds / args.steps,

@@ -171,10 +171,13 @@ int spock_set_tuning(spock_solver s, const int *in3);
  *   s: a solver created with batch 1;  x0: the initial state in the solver's (preconditioned)
  *   coordinates, nx device values;  prim_ux: device array [u (nu x numNonleaf) | x (nx x
  *   numNodes)] in the solver precision, the head of a primal vector, overwritten with the
- *   projection;  stream: a cudaStream_t (NULL for the default stream); returns when done.
+ *   projection;  stream: a cudaStream_t (NULL for the default stream); returns when done (it
+ *   synchronises the stream, unless the stream is capturing).  The caller's current device is
+ *   the same after the call as before it.
  * Problems whose workspaces (nx*numNodes + nu*numNonleaf values) exceed 8 MiB are rejected
- * with SPOCK_E_INVALID.  The first call on a device looks up the buffer's device address, so
- * make that first call before any stream capture.  All calls share the one buffer: calls that
+ * with SPOCK_E_INVALID.  The first call on a device looks up the buffer's device address (with
+ * the CUDA runtime's lazy module loading, that is also when the 8 MiB are placed on the
+ * device), so make that first call before any stream capture.  All calls share the one buffer: calls that
  * overlap on the GPU (other threads, other streams) race with each other. */
 int spock_project_dynamics_noalloc(spock_solver s, const void *x0, void *prim_ux, void *stream);
 

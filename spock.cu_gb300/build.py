@@ -14,7 +14,19 @@ SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libspock_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["engine.cu", "problem.cpp", "capi.cpp", "noalloc.cu", "offline.cu", "mlp.cu"]
+SOURCES = ["engine.cu", "problem.cpp", "capi.cpp", "noalloc.cu", "offline.cu", "mlp.cu", "ops_batch.cu"]
+# ops_batch.cu is compiled once per batched operator kernel, precision and mode
+OPS_VARIANTS = [(k, t, m) for k in ("LSTAR", "LOP") for t in ("float", "double") for m in (0, 1, 2)]
+
+
+def _jobs():
+    jobs = [(s, [], s + ".o") for s in SOURCES if s != "ops_batch.cu"]
+    for k, t, m in OPS_VARIANTS:
+        jobs.append(("ops_batch.cu", [f"-DSPOCK_OPS_{k}", f"-DSPOCK_OPS_T={t}", f"-DSPOCK_OPS_MODE={m}"],
+                     f"ops_{k.lower()}_{t}_{m}.o"))
+    # the slowest units first
+    jobs.sort(key=lambda j: (not j[0].startswith("ops"), j[0] != "engine.cu"))
+    return jobs
 
 
 def nvcc():
@@ -24,10 +36,11 @@ def nvcc():
     raise RuntimeError("nvcc not found")
 
 
-def _compile(src):
-    obj = os.path.join(OUT, os.path.basename(src) + ".o")
+def _compile(job):
+    src, defs, name = job
+    obj = os.path.join(OUT, name)
     cmd = [nvcc(), "-c", os.path.join(SRC, src), "-o", obj, "-std=c++17", "-O3", "-lineinfo",
-           "-Xcompiler", "-fPIC,-O3", "--expt-relaxed-constexpr"] + ARCH
+           "-Xcompiler", "-fPIC,-O3", "--expt-relaxed-constexpr"] + defs + ARCH
     if src.endswith(".cpp"):
         cmd[1:1] = ["-x", "cu"]
     subprocess.check_call(cmd)
@@ -43,8 +56,9 @@ def build(verbose=False):
         newest = max(os.path.getmtime(f) for f in srcs + hdrs)
         if os.path.getmtime(LIB) >= newest:
             return LIB
-    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(_compile, SOURCES))
+    jobs = _jobs()
+    with cf.ThreadPoolExecutor(max_workers=min(len(jobs), max(2, os.cpu_count() or 2))) as ex:
+        objs = list(ex.map(_compile, jobs))
     subprocess.check_call([nvcc(), "-shared", "-o", LIB + ".tmp"] + objs + ARCH + ["-lcudart"])
     os.replace(LIB + ".tmp", LIB)
     return LIB

@@ -50,10 +50,31 @@ struct RedArgs {
     long rowsPerChunk;
 };
 
+// Rows a thread sums in the solver precision before adding the block's sum into its running
+// sum.  Blocked summation (Higham, "Accuracy and Stability of Numerical Algorithms", 2nd ed.,
+// section 4.2) bounds the error by about (kRedBlock - 1) u times the sum of magnitudes when the
+// running sum is kept exactly enough.  In FP32 solvers the running sum is a float pair (hi, lo)
+// updated by Knuth's TwoSum, which carries about twice the float precision (GB300's FP64 rate is
+// ~1/64 of its FP32 rate, too slow for FP64 arithmetic per row or per block); in FP64 solvers it
+// is a double.  The pairs are widened to FP64 once per thread, before the lanes are combined.
+constexpr int kRedBlock = 32;
+
+__device__ __forceinline__ void runningAdd(float &hi, float &lo, float x) {
+    const float s = __fadd_rn(hi, x), z = __fsub_rn(s, hi);
+    lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(s, z)), __fsub_rn(x, z)));
+    hi = s;
+}
+__device__ __forceinline__ void runningAdd(double &hi, double &, double x) { hi += x; }
+
+// Per-instance partial reductions over one chunk of rows: r.Mr, max|Mr|, Mr.d (line search),
+// and in phase A the Anderson quantities c.c, c.r, c.R_s and R_s.r with c = r - r_prev.
+// Threads are TB instances x `lanes` row lanes; the lanes' FP64 sums are combined by a tree in
+// shared memory (log2(lanes) steps).
 template <typename T>
 __global__ void __launch_bounds__(kRedThreads) k_reduce(const Dims Dm, const RedArgs<T> A) {
     extern __shared__ __align__(16) unsigned char smraw[];
     double *sred = reinterpret_cast<double *>(smraw);  // [nv][lanes][TB]
+    constexpr int NV = kNV0 + 2 * kMaxAnderson;
     const int B = Dm.B;
     const int TB = B >= 32 ? 32 : B;
     const int lb = threadIdx.x % TB, lane = threadIdx.x / TB, lanes = kRedThreads / TB;
@@ -64,9 +85,9 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce(const Dims Dm, const Red
     const long k0 = (long)chunk * A.rowsPerChunk;
     const long k1 = k0 + A.rowsPerChunk < Dm.sZ ? k0 + A.rowsPerChunk : Dm.sZ;
     // accumulators indexed only by compile-time constants so they stay in registers
-    T acc[kNV0 + 2 * kMaxAnderson];
+    T hi[NV], lo[NV];
 #pragma unroll
-    for (int v = 0; v < kNV0 + 2 * kMaxAnderson; v++) acc[v] = 0;
+    for (int v = 0; v < NV; v++) hi[v] = lo[v] = 0;
     T amax = 0;
     const int ph = act ? A.phase[b] : 1;
     const bool running = act && A.status[b] == -1;
@@ -74,42 +95,60 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce(const Dims Dm, const Red
     const bool wantB = running && A.algo == kSpock && ph == 1;
     const size_t slot = (size_t)Dm.sZ * B;
     if (running) {
-#pragma unroll 2
-        for (long k = k0 + lane; k < k1; k += lanes) {
-            const size_t o = ix(k, B, b);
-            const T r = A.R[o], mr = A.MR[o];
-            acc[0] += r * mr;
-            amax = fmax(amax, fabs(mr));
-            if (wantB) acc[2] += mr * A.D[o];
-            if (wantA) {
-                const T c = r - A.RPREV[o];
-                acc[3] += c * c;
-                acc[4] += c * r;
+        for (long kb = k0 + lane; kb < k1; kb += (long)kRedBlock * lanes) {
+            const long ke = kb + (long)kRedBlock * lanes < k1 ? kb + (long)kRedBlock * lanes : k1;
+            T blk[NV];
 #pragma unroll
-                for (int s = 0; s < kMaxAnderson; s++) {
-                    if (s < A.m) {
-                        const T a = A.ANDR[s * slot + o];
-                        acc[kNV0 + s] += c * a;
-                        acc[kNV0 + kMaxAnderson + s] += a * r;
+            for (int v = 0; v < NV; v++) blk[v] = 0;
+#pragma unroll 2
+            for (long k = kb; k < ke; k += lanes) {
+                const size_t o = ix(k, B, b);
+                const T r = A.R[o], mr = A.MR[o];
+                blk[0] += r * mr;
+                amax = fmax(amax, fabs(mr));
+                if (wantB) blk[2] += mr * A.D[o];
+                if (wantA) {
+                    const T c = r - A.RPREV[o];
+                    blk[3] += c * c;
+                    blk[4] += c * r;
+#pragma unroll
+                    for (int s = 0; s < kMaxAnderson; s++) {
+                        if (s < A.m) {
+                            const T a = A.ANDR[s * slot + o];
+                            blk[kNV0 + s] += c * a;
+                            blk[kNV0 + kMaxAnderson + s] += a * r;
+                        }
                     }
                 }
             }
+            runningAdd(hi[0], lo[0], blk[0]);
+            if (wantB) runningAdd(hi[2], lo[2], blk[2]);
+            if (wantA) {
+#pragma unroll
+                for (int v = 3; v < NV; v++) runningAdd(hi[v], lo[v], blk[v]);
+            }
         }
     }
-    acc[1] = amax;
+    hi[1] = amax;
+    lo[1] = 0;
     if (laneOk)
 #pragma unroll
-        for (int v = 0; v < kNV0 + 2 * kMaxAnderson; v++) sred[(v * lanes + lane) * TB + lb] = (double)acc[v];
+        for (int v = 0; v < NV; v++) sred[(v * lanes + lane) * TB + lb] = (double)hi[v] + (double)lo[v];
     __syncthreads();
-    if (act && lane == 0)
-        for (int v = 0; v < A.nv; v++) {
-            double s = 0;
-            for (int l = 0; l < lanes; l++) {
-                const double x = sred[(v * lanes + l) * TB + lb];
-                s = (v == 1) ? fmax(s, x) : s + x;
+    int half = 1;
+    while (2 * half < lanes) half *= 2;
+    for (; half >= 1; half /= 2) {  // lane l takes lane l + half (when it exists)
+        if (laneOk && lane < half && lane + half < lanes)
+            for (int v = 0; v < A.nv; v++) {
+                double *x = sred + (v * lanes + lane) * TB + lb;
+                const double y = x[half * TB];
+                *x = (v == 1) ? fmax(*x, y) : *x + y;
             }
-            A.part[((size_t)b * A.nv + v) * A.chunks + chunk] = s;  // [instance][value][chunk]
-        }
+        __syncthreads();
+    }
+    if (act && lane == 0)
+        for (int v = 0; v < A.nv; v++)
+            A.part[((size_t)b * A.nv + v) * A.chunks + chunk] = sred[(v * lanes) * TB + lb];  // [instance][value][chunk]
 }
 
 // ------------------------------------------------------------------------------------------ controller
@@ -909,7 +948,9 @@ public:
                                                                                        stageFrom_[st], nullptr, nullptr);
             CK(cudaGetLastError());
         }
-        CK(cudaStreamSynchronize(stream));
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        CK(cudaStreamIsCapturing(stream, &cs));
+        if (cs == cudaStreamCaptureStatusNone) CK(cudaStreamSynchronize(stream));  // a capturing stream cannot wait
     }
 
     int launchesPerRound() const override { return 2 * (D_.ns - 1) + 2 + 2 + 4; }
@@ -1176,15 +1217,22 @@ private:
         CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     }
 
+    // The same through a launcher translation unit's cudaFuncSetAttribute.
+    void optInBytes(cudaError_t (*setter)(int), size_t bytes) {
+        if (bytes <= 40 * 1024) return;
+        if (bytes > 227 * 1024) throw std::invalid_argument("[Cache] problem too large for the shared-memory tiles");
+        CK(setter((int)bytes));
+    }
+
     void raiseSharedLimits() {
         if (batched_) {
             // the limit covers the largest shape the tuner may pick
-            optIn(k_lstar_b<T, 0>, bLstar(canDblLstar()));
-            optIn(k_lstar_b<T, 1>, bLstar(canDblLstar()));
-            optIn(k_lstar_b<T, 2>, bLstar(canDblLstar()));
-            optIn(k_lop_b<T, 0>, bLop(canDblLop()));
-            optIn(k_lop_b<T, 1>, bLop(canDblLop()));
-            optIn(k_lop_b<T, 2>, bLop(canDblLop()));
+            optInBytes(optInLstarB<T, 0>, bLstar(canDblLstar()));
+            optInBytes(optInLstarB<T, 1>, bLstar(canDblLstar()));
+            optInBytes(optInLstarB<T, 2>, bLstar(canDblLstar()));
+            optInBytes(optInLopB<T, 0>, bLop(canDblLop()));
+            optInBytes(optInLopB<T, 1>, bLop(canDblLop()));
+            optInBytes(optInLopB<T, 2>, bLop(canDblLop()));
             optIn(k_dyn_back_b<T>, bBack(canDblBack()));
             optIn(k_dyn_fwd_b<T>, bFwd(canDblFwd()));
             return;
@@ -1345,8 +1393,7 @@ private:
     template <int MODE>
     void launchLstar(const OpArgs<T> &A) {
         if (batched_) {
-            k_lstar_b<T, MODE><<<opGrid(tpcLstar_), kTileB * kTileWarps, smLstarB(), stream_>>>(P_, D_, A, M_, tpcLstar_,
-                                                                                                (int)lstarDbl_);
+            launchLstarB<T, MODE>(opGrid(tpcLstar_), smLstarB(), stream_, P_, D_, A, M_, tpcLstar_, (int)lstarDbl_);
             CK(cudaGetLastError());
             return;
         }
@@ -1357,8 +1404,7 @@ private:
     template <int MODE>
     void launchLop(const OpArgs<T> &A) {
         if (batched_) {
-            k_lop_b<T, MODE><<<opGrid(tpcLop_), kTileB * kTileWarps, smLopB(), stream_>>>(P_, D_, A, M_, tpcLop_,
-                                                                                          (int)lopDbl_);
+            launchLopB<T, MODE>(opGrid(tpcLop_), smLopB(), stream_, P_, D_, A, M_, tpcLop_, (int)lopDbl_);
             CK(cudaGetLastError());
             return;
         }

@@ -227,8 +227,37 @@ __global__ void __launch_bounds__(kNodeThreads) k_dyn_back(const DevProblem<T> P
     }
 }
 
+// Row r of a column-major matrix (column stride ld) times [v1 (n1 values); v2 (n2 values)]
+// (vector entries `vs` apart), plus d.  FP64: plain accumulation starting from d.  FP32: Dot2
+// (Ogita, Rump and Oishi, SIAM J. Sci. Comput. 26, 2005), with every product's exact error from
+// an FMA and every sum's from Knuth's TwoSum, for the reasons given at k_dyn_fwd_b.
+__device__ __forceinline__ double rolloutDot(const double *M, int ld, const double *v1, int vs, int n1, const double *v2,
+                                             int n2, double d) {
+    double acc = d;
+    for (int c = 0; c < n1; c++) acc += M[(size_t)c * ld] * v1[c * vs];
+    for (int c = 0; c < n2; c++) acc += M[(size_t)(n1 + c) * ld] * v2[c * vs];
+    return acc;
+}
+__device__ __forceinline__ void twoSumAcc(float &s, float &cmp, float m, float v) {
+    const float h = __fmul_rn(m, v), pe = __fmaf_rn(m, v, -h);
+    const float t = __fadd_rn(s, h), z = __fsub_rn(t, s);
+    const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(h, z));
+    cmp = __fadd_rn(cmp, __fadd_rn(e, pe));
+    s = t;
+}
+__device__ __forceinline__ float rolloutDot(const float *M, int ld, const float *v1, int vs, int n1, const float *v2, int n2,
+                                            float d) {
+    float s = 0.f, cmp = 0.f;
+    for (int c = 0; c < n1; c++) twoSumAcc(s, cmp, M[(size_t)c * ld], v1[c * vs]);
+    for (int c = 0; c < n2; c++) twoSumAcc(s, cmp, M[(size_t)(n1 + c) * ld], v2[c * vs]);
+    const float h = __fadd_rn(s, d), z = __fsub_rn(h, s);
+    const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(h, z)), __fsub_rn(d, z));
+    return __fadd_rn(h, __fadd_rn(e, cmp));
+}
+
 // ------------------------------------------------------------------------------------------
-// Dynamics projection, forward rollout for one stage (dynamics.cuh:143-173).
+// Dynamics projection, forward rollout for one stage (dynamics.cuh:143-173), compensated in
+// FP32 (rolloutDot).
 // ------------------------------------------------------------------------------------------
 template <typename T>
 __global__ void __launch_bounds__(kNodeThreads) k_dyn_fwd(const DevProblem<T> P, const Dims D, T *__restrict__ cand,
@@ -259,9 +288,8 @@ __global__ void __launch_bounds__(kNodeThreads) k_dyn_fwd(const DevProblem<T> P,
     __syncthreads();
     if (act)
         for (int r = rg; r < nu; r += RG) {
-            T acc = DD[ix((long)i * nu + r, B, b)];
-            const T *M = P.K + (size_t)i * nu * nx + r;
-            for (int c = 0; c < nx; c++) acc += M[(size_t)c * nu] * sx[c * TB + lb];
+            const T acc = rolloutDot(P.K + (size_t)i * nu * nx + r, nu, sx + lb, TB, nx, nullptr, 0,
+                                     DD[ix((long)i * nu + r, B, b)]);
             su[r * TB + lb] = acc;
             cand[ix((long)i * nu + r, B, b)] = acc;
             if (R) R[ix((long)i * nu + r, B, b)] = Z[ix((long)i * nu + r, B, b)] - acc;
@@ -272,9 +300,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_dyn_fwd(const DevProblem<T> P,
     for (int t = rg; t < nc * nx; t += RG) {
         const int jj = t / nx, r = t % nx, j = c0 + jj;
         const T *M = P.AB + (size_t)j * nx * nxu + r;
-        T acc = D.affine ? P.e[(size_t)j * nx + r] : T(0);
-        for (int c = 0; c < nx; c++) acc += M[(size_t)c * nx] * sx[c * TB + lb];
-        for (int c = 0; c < nu; c++) acc += M[(size_t)(nx + c) * nx] * su[c * TB + lb];
+        const T acc = rolloutDot(M, nx, sx + lb, TB, nx, su + lb, nu, D.affine ? P.e[(size_t)j * nx + r] : T(0));
         cand[ix(D.oX + (long)j * nx + r, B, b)] = acc;
         if (R) R[ix(D.oX + (long)j * nx + r, B, b)] = Z[ix(D.oX + (long)j * nx + r, B, b)] - acc;
     }

@@ -156,6 +156,74 @@ __device__ __forceinline__ void gemv(T acc[kMaxTasks][kRT], const T *M, int rows
     }
 }
 
+// Compensated matrix-vector accumulation for the forward rollout of the dynamics projection.
+// Algorithm Dot2 of Ogita, Rump and Oishi ("Accurate sum and dot product", SIAM J. Sci.
+// Comput. 26, 2005): every product m*v is split into its rounded value h and its exact error
+// fma(m, v, -h); h is added to the running sum by Knuth's TwoSum, whose exact error goes, with
+// the product's, into a second accumulator.  acc + cmp is then the dot product as accurate as
+// if it had been accumulated in twice the working precision.  In FP32 each step is ten packed
+// two-lane instructions (rounded to nearest, never contracted: inline PTX); in FP64 it is the
+// plain FMA and cmp stays zero.
+__device__ __forceinline__ unsigned long long pack2(float a, float b) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void unpack2(unsigned long long r, float &a, float &b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ void axpy16c(float acc[kRT], float cmp[kRT], const float m[kRT], float v) {
+    const unsigned long long vv = pack2(v, v), nv = pack2(-v, -v);
+#pragma unroll
+    for (int t = 0; t < kRT; t += 2) {
+        const unsigned long long a = pack2(acc[t], acc[t + 1]), mm = pack2(m[t], m[t + 1]);
+        unsigned long long c = pack2(cmp[t], cmp[t + 1]);
+        unsigned long long nh, pe, s, z, t1, t2, t3, e;
+        asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(nh) : "l"(mm), "l"(nv));         // -h, h = fl(m v)
+        asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(pe) : "l"(mm), "l"(vv), "l"(nh));  // m v - h exactly
+        asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(s) : "l"(a), "l"(nh));           // s = fl(a + h)
+        asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(z) : "l"(s), "l"(a));            // TwoSum(a, h)
+        asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(t1) : "l"(s), "l"(z));
+        asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(t2) : "l"(a), "l"(t1));          // a - (s - z)
+        asm("add.rn.f32x2 %0, %1, %2;" : "=l"(t3) : "l"(nh), "l"(z));          // -(h - z)
+        asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(e) : "l"(t2), "l"(t3));          // a + h - s exactly
+        asm("add.rn.f32x2 %0, %1, %2;" : "=l"(e) : "l"(e), "l"(pe));
+        asm("add.rn.f32x2 %0, %1, %2;" : "=l"(c) : "l"(c), "l"(e));
+        unpack2(s, acc[t], acc[t + 1]);
+        unpack2(c, cmp[t], cmp[t + 1]);
+    }
+}
+__device__ __forceinline__ void axpy16c(double acc[kRT], double *, const double m[kRT], double v) { axpy16(acc, m, v); }
+
+// The compensated sum's value plus an addend d: TwoSum(s, d), then both errors (FP32), or
+// s + d (FP64, where the compensation is not used).
+__device__ __forceinline__ float finishc(float s, float c, float d) {
+    const float h = __fadd_rn(s, d), z = __fsub_rn(h, s);
+    const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(h, z)), __fsub_rn(d, z));
+    return __fadd_rn(h, __fadd_rn(e, c));
+}
+__device__ __forceinline__ double finishc(double s, double, double d) { return s + d; }
+
+// gemv with Dot2 accumulation, one matrix column per step.
+template <typename T, typename In>
+__device__ __forceinline__ void gemvc(T acc[kMaxTasks][kRT], T cmp[kMaxTasks][kRT], const T *M, int rows, int K, int slot,
+                                      In in) {
+    const int ld = pad16(rows);
+    const int nTasks = ld / kRT;
+#pragma unroll
+    for (int q = 0; q < kMaxTasks; q++) {
+        const int task = slot + q * kTileWarps;
+        if (task >= nTasks) continue;
+        const T *col = M + task * kRT;
+#pragma unroll 1
+        for (int k = 0; k < K; k++) {
+            T m0[kRT];
+            load16(col + (size_t)k * ld, m0);
+            axpy16c(acc[q], cmp[q], m0, in(k));
+        }
+    }
+}
+
 // Gather rows rowOf(0..n-1) of `src` for instances b0 .. b0+31 into sm[r*32 + lane].
 template <typename T, typename RowOf>
 __device__ __forceinline__ void gather(T *sm, int n, const T *src, int B, int b0, int lane, int warp, RowOf rowOf) {
@@ -939,7 +1007,11 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, 2) k_dyn_back_b(const DevP
 
 // ------------------------------------------------------------------------------------------
 // Dynamics projection, one stage of the forward rollout (dynamics.cuh:143-173), writing the
-// candidate (x, u) and its residual Z - cand.  Tiles as in k_dyn_back_b.
+// candidate (x, u) and its residual Z - cand.  Tiles as in k_dyn_back_b.  Both products,
+// u = K x + d and x+ = [A B][x; u] (+ e), are Dot2-compensated in FP32: the rollout is ten
+// stages deep, and plain float accumulation there leaves errors (~1e-6 relative) that change
+// from one T evaluation to the next and spoil the residual differences Anderson and the
+// SuperMann tests compare.
 // ------------------------------------------------------------------------------------------
 template <typename T>
 __global__ void __launch_bounds__(kTileB *kTileWarps, 2) k_dyn_fwd_b(const DevProblem<T> P, const Dims D, const PadMats<T> M,
@@ -998,9 +1070,10 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, 2) k_dyn_fwd_b(const DevPr
                 cand[ix(D.oX + r, B, b)] = x;
                 if (R) R[ix(D.oX + r, B, b)] = sz[(nu + nc * nx + r) * kTileB + lane] - x;
             }
-        T acc[kMaxTasks][kRT];
+        T acc[kMaxTasks][kRT], cmp[kMaxTasks][kRT];  // Dot2 sums (gemvc): the rollout is compensated
         zeroAcc(acc);
-        gemv(acc, sK, nu, nx, warp, [&](int k) { return sxu[k * kTileB + lane]; });
+        zeroAcc(cmp);
+        gemvc(acc, cmp, sK, nu, nx, warp, [&](int k) { return sxu[k * kTileB + lane]; });
 #pragma unroll
         for (int q = 0; q < kMaxTasks; q++) {
             const int r0 = (warp + q * kTileWarps) * kRT;
@@ -1008,7 +1081,7 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, 2) k_dyn_fwd_b(const DevPr
             for (int t = 0; t < kRT; t++) {
                 const int r = r0 + t;
                 if (r < nu) {
-                    const T u = acc[q][t] + sdd[r * kTileB + lane];
+                    const T u = finishc(acc[q][t], cmp[q][t], sdd[r * kTileB + lane]);
                     sxu[(nx + r) * kTileB + lane] = u;
                     if (act) {
                         cand[ix((long)i * nu + r, B, b)] = u;
@@ -1021,8 +1094,9 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, 2) k_dyn_fwd_b(const DevPr
         for (int jj = 0; jj < nc; jj++) {
             const int j = c0 + jj;
             zeroAcc(acc);
+            zeroAcc(cmp);
             const int slot = slotFrom(warp, jj * tasksOf(nx));  // children's blocks on different warps
-            gemv(acc, sAB + jj * ldx * nxu, nx, nxu, slot, [&](int k) { return sxu[k * kTileB + lane]; });
+            gemvc(acc, cmp, sAB + jj * ldx * nxu, nx, nxu, slot, [&](int k) { return sxu[k * kTileB + lane]; });
             if (!act) continue;
 #pragma unroll
             for (int q = 0; q < kMaxTasks; q++) {
@@ -1031,7 +1105,7 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, 2) k_dyn_fwd_b(const DevPr
                 for (int t = 0; t < kRT; t++) {
                     const int r = r0 + t;
                     if (r < nx) {
-                        const T x = acc[q][t] + (D.affine ? P.e[(size_t)j * nx + r] : T(0));
+                        const T x = finishc(acc[q][t], cmp[q][t], D.affine ? P.e[(size_t)j * nx + r] : T(0));
                         cand[ix(D.oX + (long)j * nx + r, B, b)] = x;
                         if (R) R[ix(D.oX + (long)j * nx + r, B, b)] = sz[(nu + jj * nx + r) * kTileB + lane] - x;
                     }
@@ -1044,5 +1118,24 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, 2) k_dyn_fwd_b(const DevPr
         if (!dbl && tile + 1 < t1) prefetch(tile + 1);
     }
 }
+
+}  // namespace spock
+
+namespace spock {
+
+// Host-side launchers of the two largest kernels.  Each (kernel, precision, mode) is compiled in
+// a translation unit of its own (ops_batch.cu, built once per combination), so their device
+// code compiles in parallel; the engine calls these instead of launching the kernels itself.
+template <typename T, int MODE>
+void launchLstarB(dim3 grid, size_t smem, cudaStream_t stream, const DevProblem<T> &P, const Dims &D, const OpArgs<T> &A,
+                  const PadMats<T> &M, int tilesPerCta, int dbl);
+template <typename T, int MODE>
+void launchLopB(dim3 grid, size_t smem, cudaStream_t stream, const DevProblem<T> &P, const Dims &D, const OpArgs<T> &A,
+                const PadMats<T> &M, int tilesPerCta, int dbl);
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) of the same kernels.
+template <typename T, int MODE>
+cudaError_t optInLstarB(int bytes);
+template <typename T, int MODE>
+cudaError_t optInLopB(int bytes);
 
 }  // namespace spock

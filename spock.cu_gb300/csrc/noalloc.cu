@@ -26,7 +26,9 @@ void *g_scratchAddr[kMaxDevices] = {};
 std::mutex g_scratchMutex;
 
 // Device address of the buffer on the current device, looked up once per device.  In host
-// code g_spockDynScratch names a host-side stand-in, never the device memory itself.
+// code g_spockDynScratch names a host-side stand-in, never the device memory itself.  The
+// cached address stays valid while the device's primary context lives; a process that resets
+// the device (cudaDeviceReset) must not call this entry point afterwards.
 void *scratchOnCurrentDevice() {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -43,14 +45,31 @@ void *scratchOnCurrentDevice() {
     return g_scratchAddr[dev];
 }
 
+// Makes `device` current for the call and gives the caller back its own current device after.
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int device) {
+        cudaError_t e = cudaGetDevice(&prev);
+        if (e != cudaSuccess) throw std::runtime_error(std::string("[noalloc] cudaGetDevice: ") + cudaGetErrorString(e));
+        if (prev != device) {
+            e = cudaSetDevice(device);
+            if (e != cudaSuccess)
+                throw std::runtime_error(std::string("[noalloc] cudaSetDevice: ") + cudaGetErrorString(e));
+        }
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        if (cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
 }  // namespace
 
 extern "C" int spock_project_dynamics_noalloc(spock_solver s, const void *x0, void *prim_ux, void *stream) {
     return spock::guardedCall([&] {
         spock::EngineBase *eng = spock::engineOf(s);
         if (!x0 || !prim_ux) throw std::invalid_argument("[noalloc] null device pointer");
-        cudaError_t e = cudaSetDevice(eng->device());
-        if (e != cudaSuccess) throw std::runtime_error(std::string("[noalloc] cudaSetDevice: ") + cudaGetErrorString(e));
+        DeviceGuard guard(eng->device());
         void *scratch = scratchOnCurrentDevice();
         // nothing in the buffer needs to start at zero: the sweep writes every workspace entry
         // before it reads it

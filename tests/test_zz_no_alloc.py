@@ -38,15 +38,25 @@ def test_no_alloc_projection_matches_cp_step(case, precision, tol):
     x0 = golden(case, "initialState_d.bt")
     x0s = torch.tensor(x0 * d.scaling()[:nx], dtype=dt, device="cuda")
     rng = np.random.default_rng(17)
+    side = torch.cuda.Stream()
     for call in range(2):  # two calls in a row share the static workspace
         z = np.zeros(c.sizeIterate())
         z[:head] = 3 * rng.standard_normal(head)
         ref = c.cpStep(x0, z)[:head]  # existing entry point
         buf = torch.tensor(z[:head], dtype=dt, device="cuda")
         torch.cuda.synchronize()
+        # the second call runs on a caller-created stream, and device memory in use must not
+        # change across it (the first call may load the library's module holding the static
+        # buffer: with lazy module loading the CUDA runtime places the buffer then)
+        stream = None if call == 0 else ctypes.c_void_p(side.cuda_stream)
+        free_before = torch.cuda.mem_get_info()[0]
         rc = sg.lib().spock_project_dynamics_noalloc(c._h, ctypes.c_void_p(x0s.data_ptr()),
-                                                      ctypes.c_void_p(buf.data_ptr()), None)
+                                                      ctypes.c_void_p(buf.data_ptr()), stream)
+        free_after = torch.cuda.mem_get_info()[0]
         assert rc == 0, sg.lib().spock_last_error().decode()
+        if call > 0:
+            assert free_after == free_before, (free_before, free_after)
+        torch.cuda.synchronize()
         out = buf.cpu().double().numpy()
         assert np.abs(out - ref).max() <= tol * max(1., np.abs(ref).max()), call
 
