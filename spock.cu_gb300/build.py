@@ -15,15 +15,15 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libspock_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["engine.cu", "problem.cpp", "capi.cpp", "noalloc.cu", "offline.cu", "mlp.cu", "ops_batch.cu"]
-# ops_batch.cu is compiled once per batched operator kernel, precision and mode
-OPS_VARIANTS = [(k, t, m) for k in ("LSTAR", "LOP") for t in ("float", "double") for m in (0, 1, 2)]
+# ops_batch.cu is compiled once per batched operator kernel, precision, mode and matrix placement
+OPS_VARIANTS = [(k, t, m, g) for k in ("LSTAR", "LOP") for t in ("float", "double") for m in (0, 1, 2) for g in (0, 1)]
 
 
 def _jobs():
     jobs = [(s, [], s + ".o") for s in SOURCES if s != "ops_batch.cu"]
-    for k, t, m in OPS_VARIANTS:
-        jobs.append(("ops_batch.cu", [f"-DSPOCK_OPS_{k}", f"-DSPOCK_OPS_T={t}", f"-DSPOCK_OPS_MODE={m}"],
-                     f"ops_{k.lower()}_{t}_{m}.o"))
+    for k, t, m, g in OPS_VARIANTS:
+        jobs.append(("ops_batch.cu", [f"-DSPOCK_OPS_{k}", f"-DSPOCK_OPS_T={t}", f"-DSPOCK_OPS_MODE={m}",
+                                      f"-DSPOCK_OPS_GM={g}"], f"ops_{k.lower()}_{t}_{m}_{g}.o"))
     # the slowest units first
     jobs.sort(key=lambda j: (not j[0].startswith("ops"), j[0] != "engine.cu"))
     return jobs

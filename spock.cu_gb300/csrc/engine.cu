@@ -19,6 +19,7 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 
 #include "engine.cuh"
 #include "kernels.cuh"
@@ -70,11 +71,15 @@ __device__ __forceinline__ void runningAdd(double &hi, double &, double x) { hi 
 // and in phase A the Anderson quantities c.c, c.r, c.R_s and R_s.r with c = r - r_prev.
 // Threads are TB instances x `lanes` row lanes; the lanes' FP64 sums are combined by a tree in
 // shared memory (log2(lanes) steps).
-template <typename T>
+// M = the Anderson memory (A.m), a template parameter so that only the 5 + 2M accumulators in
+// use occupy registers; the partials keep slots kNV0 + s and kNV0 + kMaxAnderson + s for the
+// Anderson products whatever M is.
+template <typename T, int M>
 __global__ void __launch_bounds__(kRedThreads) k_reduce(const Dims Dm, const RedArgs<T> A) {
     extern __shared__ __align__(16) unsigned char smraw[];
     double *sred = reinterpret_cast<double *>(smraw);  // [nv][lanes][TB]
-    constexpr int NV = kNV0 + 2 * kMaxAnderson;
+    constexpr int NV = kNV0 + 2 * M;                  // accumulator k goes to partials slot slotOf(k)
+    auto slotOf = [](int k) { return k < kNV0 + M ? k : k - M + kMaxAnderson; };
     const int B = Dm.B;
     const int TB = B >= 32 ? 32 : B;
     const int lb = threadIdx.x % TB, lane = threadIdx.x / TB, lanes = kRedThreads / TB;
@@ -100,7 +105,7 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce(const Dims Dm, const Red
             T blk[NV];
 #pragma unroll
             for (int v = 0; v < NV; v++) blk[v] = 0;
-#pragma unroll 2
+#pragma unroll 4
             for (long k = kb; k < ke; k += lanes) {
                 const size_t o = ix(k, B, b);
                 const T r = A.R[o], mr = A.MR[o];
@@ -112,12 +117,10 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce(const Dims Dm, const Red
                     blk[3] += c * c;
                     blk[4] += c * r;
 #pragma unroll
-                    for (int s = 0; s < kMaxAnderson; s++) {
-                        if (s < A.m) {
-                            const T a = A.ANDR[s * slot + o];
-                            blk[kNV0 + s] += c * a;
-                            blk[kNV0 + kMaxAnderson + s] += a * r;
-                        }
+                    for (int s = 0; s < M; s++) {
+                        const T a = A.ANDR[s * slot + o];
+                        blk[kNV0 + s] += c * a;
+                        blk[kNV0 + M + s] += a * r;
                     }
                 }
             }
@@ -131,9 +134,12 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce(const Dims Dm, const Red
     }
     hi[1] = amax;
     lo[1] = 0;
-    if (laneOk)
+    if (laneOk) {
 #pragma unroll
-        for (int v = 0; v < NV; v++) sred[(v * lanes + lane) * TB + lb] = (double)hi[v] + (double)lo[v];
+        for (int v = 0; v < NV; v++) sred[(slotOf(v) * lanes + lane) * TB + lb] = (double)hi[v] + (double)lo[v];
+        for (int v = kNV0 + M; v < kNV0 + kMaxAnderson; v++) sred[(v * lanes + lane) * TB + lb] = 0;
+        for (int v = kNV0 + kMaxAnderson + M; v < A.nv; v++) sred[(v * lanes + lane) * TB + lb] = 0;
+    }
     __syncthreads();
     int half = 1;
     while (2 * half < lanes) half *= 2;
@@ -340,8 +346,11 @@ struct UpdArgs {
     int m;
 };
 
-template <typename T>
-__global__ void __launch_bounds__(256) k_update(const Dims Dm, const UpdArgs<T> A) {
+// M = the Anderson memory (A.m) as a template parameter: the coefficients and the loop over the
+// memory's columns are sized at compile time.  Four CTAs of 256 threads per SM (at most 64
+// registers a thread) keep enough loads in flight for HBM.
+template <typename T, int M>
+__global__ void __launch_bounds__(256, 4) k_update(const Dims Dm, const UpdArgs<T> A) {
     // thread = instance b (x) and a stride of rows (y): consecutive lanes touch consecutive
     // instances of a row (coalesced), the action is read once, and the row loop is unrolled over
     // non-aliasing pointers so several rows' loads are in flight per thread
@@ -362,15 +371,14 @@ __global__ void __launch_bounds__(256) k_update(const Dims Dm, const UpdArgs<T> 
         T *__restrict__ D = A.D;
         T *__restrict__ ANDR = A.ANDR;
         T *__restrict__ ANDZ = A.ANDZ;
-        const int m = A.m;
-        const int h = (A.head[b] + m - 1) % m;  // slot written this round (head already advanced)
-        T g[kMaxAnderson];
+        const int h = (A.head[b] + M - 1) % M;  // slot written this round (head already advanced)
+        T g[M];
         const bool useAnd = A.useAnd[b];
 #pragma unroll
-        for (int s2 = 0; s2 < kMaxAnderson; s2++)
-            g[s2] = (useAnd && s2 < m && s2 != h) ? T(A.gamma[(size_t)b * kMaxAnderson + s2]) : T(0);
+        for (int s2 = 0; s2 < M; s2++)
+            g[s2] = (useAnd && s2 != h) ? T(A.gamma[(size_t)b * kMaxAnderson + s2]) : T(0);
         const T gh = useAnd ? T(A.gamma[(size_t)b * kMaxAnderson + h]) : T(0);
-#pragma unroll 4
+#pragma unroll 2
         for (long k = k0; k < n; k += step) {
             const size_t o = (size_t)k * B + b;
             const T z = Z[o], r = R[o], c = CAND[o];
@@ -378,8 +386,8 @@ __global__ void __launch_bounds__(256) k_update(const Dims Dm, const UpdArgs<T> 
             const T dzr = (z - PREV[o]) - dr;
             T d = -r - gh * dzr;
 #pragma unroll
-            for (int s2 = 0; s2 < kMaxAnderson; s2++)
-                if (s2 < m && s2 != h) d -= g[s2] * ANDZ[s2 * slot + o];
+            for (int s2 = 0; s2 < M; s2++)
+                if (s2 != h) d -= g[s2] * ANDZ[s2 * slot + o];
             ANDR[h * slot + o] = dr;
             ANDZ[h * slot + o] = dzr;
             D[o] = d;
@@ -1092,18 +1100,23 @@ private:
                D_.conNl == kConPolyhedronWithIdentity || D_.conL == kConPolyhedronWithIdentity ||
                D_.conNl == kConRectangleInputBall;
     }
-    size_t bLstar(bool dbl = false) const {
+    // Shared memory of the batched kernels; `gm`: node matrices read in place, not staged.
+    size_t bLstar(bool dbl = false) const { return bLstar(dbl, (D_.gmat & kGmatLstar) != 0); }
+    size_t bLstar(bool dbl, bool gm) const {
         const size_t in = (size_t)std::max(D_.ne * D_.dIV + idNl() + gNl() + D_.yD + 2 + 2 * D_.ne, D_.dVI + idL() + gL());
         const size_t base = (size_t)std::max(D_.nxu + D_.yD + 2 * D_.ne + 2, D_.nx);
-        const size_t mats = std::max((size_t)D_.ne * (lx() * D_.nx + lu() * D_.nu + lx() + lu()), lx() * D_.nx + lx()) +
+        const size_t mats = gm ? 0 :
+                            std::max((size_t)D_.ne * (lx() * D_.nx + lu() * D_.nu + lx() + lu()), lx() * D_.nx + lx()) +
                             std::max((size_t)pad16(D_.nxu) * gNl(), (size_t)pad16(D_.nx) * gL());
         const size_t gv = (gNl() || gL() || D_.costNl == kCostLinear || D_.costL == kCostLinear) ? (size_t)D_.nxu : 0;
         return (mats + ((dbl ? 2 : 1) * (in + base) + (size_t)D_.nd + gv) * kTileB) * sizeof(T) + (in + base) * sizeof(int);
     }
-    size_t bLop(bool dbl = false) const {
+    size_t bLop(bool dbl = false) const { return bLop(dbl, (D_.gmat & kGmatLop) != 0); }
+    size_t bLop(bool dbl, bool gm) const {
         const size_t in = (size_t)std::max(2 * D_.nxu + D_.yD + 2, D_.nxu + D_.nx + 2);
         const size_t base = (size_t)std::max(D_.yD + 1 + idNl() + gNl() + D_.dIV, D_.dIV + idL() + gL() + D_.dVI);
-        const size_t mats = 2 * lx() * D_.nx + lu() * D_.nu +
+        const size_t mats = gm ? 0 :
+                            2 * lx() * D_.nx + lu() * D_.nu +
                             std::max((size_t)pad16(gNl()) * D_.nxu, (size_t)pad16(gL()) * D_.nx);
         return (mats + ((size_t)std::max({D_.dIV, D_.dVI, D_.nu}) + kTileWarps + (dbl ? 2 : 1) * (2 * in + base)) * kTileB) *
                    sizeof(T) +
@@ -1113,12 +1126,15 @@ private:
     size_t smLopB() const { return bLop(lopDbl_); }
     bool canDblLstar() const { return bLstar(true) <= 220 * 1024; }
     bool canDblLop() const { return bLop(true) <= 220 * 1024; }
-    size_t bBack(bool dbl = false) const {
-        const size_t mats = (size_t)D_.ne * (lu() * D_.nx + lx() * D_.nu + lx() * D_.nx) + lx() * D_.nu + lu() * D_.nu;
-        return (mats + ((dbl ? 2 : 1) * (size_t)(D_.ne * D_.nx + D_.nu + D_.nx) + D_.nu) * kTileB) * sizeof(T);
+    size_t bBack(bool dbl = false) const { return bBack(dbl, (D_.gmat & kGmatBack) != 0); }
+    size_t bBack(bool dbl, bool gm) const {
+        const size_t mats = gm ? 0 : (size_t)D_.ne * (lu() * D_.nx + lx() * D_.nu + lx() * D_.nx) + lx() * D_.nu + lu() * D_.nu;
+        const size_t dOwn = sizeof(T) == 4 && D_.nx < D_.nu ? D_.nu : 0;  // d's own rows (k_dyn_back_b)
+        return (mats + ((dbl ? 2 : 1) * (size_t)(D_.ne * D_.nx + D_.nu + D_.nx) + D_.nu + dOwn) * kTileB) * sizeof(T);
     }
-    size_t bFwd(bool dbl = false) const {
-        const size_t mats = lu() * D_.nx + (size_t)D_.ne * lx() * D_.nxu;
+    size_t bFwd(bool dbl = false) const { return bFwd(dbl, (D_.gmat & kGmatFwd) != 0); }
+    size_t bFwd(bool dbl, bool gm) const {
+        const size_t mats = gm ? 0 : lu() * D_.nx + (size_t)D_.ne * lx() * D_.nxu;
         return (mats + (dbl ? 2 : 1) * (size_t)(D_.nxu + 2 * D_.nu + D_.ne * D_.nx + D_.nx) * kTileB) * sizeof(T);
     }
     bool canDblBack() const { return bBack(true) <= 220 * 1024; }
@@ -1126,6 +1142,11 @@ private:
 
     void chooseKernels() {
         const int maxRows = kRT * kTileWarps * kMaxTasks;
+        // node matrices too large for shared memory are read in place by the kernels concerned
+        const size_t cap = 220 * 1024;
+        D_.gmat = (bLstar(false, false) > cap ? kGmatLstar : 0) | (bLop(false, false) > cap ? kGmatLop : 0) |
+                  (bBack(false, false) > cap ? kGmatBack : 0) |
+                  (bFwd(false, false) > cap ? kGmatFwd : 0);
         // linear costs and polyhedral constraints exist only in the batched kernels, which also run
         // batches below one tile (the lanes past the batch stay idle)
         const bool fits = pad16(D_.nx) <= maxRows && pad16(D_.nu) <= maxRows && pad16(D_.nxu) <= maxRows &&
@@ -1149,6 +1170,12 @@ private:
         M_.Kt = padUpload(p.K, nx, nu, p.numNonleaf, true);  // K' from K (nu x nx)
         M_.K = padUpload(p.K, nu, nx, p.numNonleaf);
         M_.chol = padUpload(p.lowChol, nu, nu, p.numNonleaf);
+        if (sizeof(T) == 4) {  // (I + sum B'PB)^-1 as a float pair hi + lo
+            std::vector<double> inv = choleskyInverses(p.lowChol, nu, p.numNonleaf), lo(inv.size());
+            for (size_t k = 0; k < inv.size(); k++) lo[k] = inv[k] - (double)(float)inv[k];
+            M_.cholInv = padUpload(inv, nu, nu, p.numNonleaf);
+            M_.cholInvLo = padUpload(lo, nu, nu, p.numNonleaf);
+        }
         M_.AB = padUpload(p.AB, nx, nx + nu, p.numNodes);
         if (gNl()) {
             M_.nlG = padUpload(p.nlGamma, gNl(), D_.nxu, 1);
@@ -1158,6 +1185,30 @@ private:
             M_.lG = padUpload(p.lGamma, gL(), nx, 1);
             M_.lGT = padUpload(p.lGamma, nx, gL(), 1, true);
         }
+    }
+
+    // (L L')^-1 of every lower Cholesky factor L (nu x nu, column-major), in FP64.
+    static std::vector<double> choleskyInverses(const std::vector<double> &chol, int nu, long mats) {
+        std::vector<double> out((size_t)nu * nu * mats), Li((size_t)nu * nu);
+        for (long m = 0; m < mats; m++) {
+            const double *L = chol.data() + (size_t)m * nu * nu;  // L(r, c) at c * nu + r
+            std::fill(Li.begin(), Li.end(), 0.);
+            for (int c = 0; c < nu; c++) {  // column c of L^-1 by forward substitution
+                for (int r = c; r < nu; r++) {
+                    double v = r == c ? 1. : 0.;
+                    for (int k = c; k < r; k++) v -= L[(size_t)k * nu + r] * Li[(size_t)c * nu + k];
+                    Li[(size_t)c * nu + r] = v / L[(size_t)r * nu + r];
+                }
+            }
+            double *O = out.data() + (size_t)m * nu * nu;
+            for (int c = 0; c < nu; c++)
+                for (int r = 0; r < nu; r++) {  // (L^-T L^-1)(r, c) = sum_k Li(k, r) Li(k, c)
+                    double v = 0;
+                    for (int k = std::max(r, c); k < nu; k++) v += Li[(size_t)r * nu + k] * Li[(size_t)c * nu + k];
+                    O[(size_t)c * nu + r] = v;
+                }
+        }
+        return out;
     }
 
     void allocate() {
@@ -1227,14 +1278,17 @@ private:
     void raiseSharedLimits() {
         if (batched_) {
             // the limit covers the largest shape the tuner may pick
-            optInBytes(optInLstarB<T, 0>, bLstar(canDblLstar()));
-            optInBytes(optInLstarB<T, 1>, bLstar(canDblLstar()));
-            optInBytes(optInLstarB<T, 2>, bLstar(canDblLstar()));
-            optInBytes(optInLopB<T, 0>, bLop(canDblLop()));
-            optInBytes(optInLopB<T, 1>, bLop(canDblLop()));
-            optInBytes(optInLopB<T, 2>, bLop(canDblLop()));
-            optIn(k_dyn_back_b<T>, bBack(canDblBack()));
-            optIn(k_dyn_fwd_b<T>, bFwd(canDblFwd()));
+            const bool gS = D_.gmat & kGmatLstar, gL = D_.gmat & kGmatLop;
+            optInBytes(gS ? optInLstarB<T, 0, true> : optInLstarB<T, 0, false>, bLstar(canDblLstar()));
+            optInBytes(gS ? optInLstarB<T, 1, true> : optInLstarB<T, 1, false>, bLstar(canDblLstar()));
+            optInBytes(gS ? optInLstarB<T, 2, true> : optInLstarB<T, 2, false>, bLstar(canDblLstar()));
+            optInBytes(gL ? optInLopB<T, 0, true> : optInLopB<T, 0, false>, bLop(canDblLop()));
+            optInBytes(gL ? optInLopB<T, 1, true> : optInLopB<T, 1, false>, bLop(canDblLop()));
+            optInBytes(gL ? optInLopB<T, 2, true> : optInLopB<T, 2, false>, bLop(canDblLop()));
+            if (D_.gmat & kGmatBack) optIn(k_dyn_back_b<T, true>, bBack(canDblBack()));
+            else optIn(k_dyn_back_b<T, false>, bBack(canDblBack()));
+            if (D_.gmat & kGmatFwd) optIn(k_dyn_fwd_b<T, true>, bFwd(canDblFwd()));
+            else optIn(k_dyn_fwd_b<T, false>, bFwd(canDblFwd()));
             return;
         }
         optIn(k_dyn_back<T>, smBack());
@@ -1393,7 +1447,10 @@ private:
     template <int MODE>
     void launchLstar(const OpArgs<T> &A) {
         if (batched_) {
-            launchLstarB<T, MODE>(opGrid(tpcLstar_), smLstarB(), stream_, P_, D_, A, M_, tpcLstar_, (int)lstarDbl_);
+            if (D_.gmat & kGmatLstar)
+                launchLstarB<T, MODE, true>(opGrid(tpcLstar_), smLstarB(), stream_, P_, D_, A, M_, tpcLstar_, (int)lstarDbl_);
+            else
+                launchLstarB<T, MODE, false>(opGrid(tpcLstar_), smLstarB(), stream_, P_, D_, A, M_, tpcLstar_, (int)lstarDbl_);
             CK(cudaGetLastError());
             return;
         }
@@ -1404,7 +1461,10 @@ private:
     template <int MODE>
     void launchLop(const OpArgs<T> &A) {
         if (batched_) {
-            launchLopB<T, MODE>(opGrid(tpcLop_), smLopB(), stream_, P_, D_, A, M_, tpcLop_, (int)lopDbl_);
+            if (D_.gmat & kGmatLop)
+                launchLopB<T, MODE, true>(opGrid(tpcLop_), smLopB(), stream_, P_, D_, A, M_, tpcLop_, (int)lopDbl_);
+            else
+                launchLopB<T, MODE, false>(opGrid(tpcLop_), smLopB(), stream_, P_, D_, A, M_, tpcLop_, (int)lopDbl_);
             CK(cudaGetLastError());
             return;
         }
@@ -1416,13 +1476,15 @@ private:
         const int N = D_.ns - 1;
         if (batched_) {
             const size_t smB = bBack(backDbl_), smF = bFwd(fwdDbl_);
+            auto back = D_.gmat & kGmatBack ? k_dyn_back_b<T, true> : k_dyn_back_b<T, false>;
+            auto fwd = D_.gmat & kGmatFwd ? k_dyn_fwd_b<T, true> : k_dyn_fwd_b<T, false>;
             for (int st = N - 1; st >= 0; st--) {
-                k_dyn_back_b<T><<<opGridNodes(tpcDyn_, stageCount_[st]), kTileB * kTileWarps, smB, stream_>>>(
+                back<<<opGridNodes(tpcDyn_, stageCount_[st]), kTileB * kTileWarps, smB, stream_>>>(
                     P_, D_, M_, CAND_, Q_, DD_, stageFrom_[st], st, tpcDyn_, (int)backDbl_, S_.tileLive);
                 CK(cudaGetLastError());
             }
             for (int st = 0; st < N; st++) {
-                k_dyn_fwd_b<T><<<opGridNodes(tpcDyn_, stageCount_[st]), kTileB * kTileWarps, smF, stream_>>>(
+                fwd<<<opGridNodes(tpcDyn_, stageCount_[st]), kTileB * kTileWarps, smF, stream_>>>(
                     P_, D_, M_, CAND_, DD_, x0s_, stageFrom_[st], Z_, R_, tpcDyn_, (int)fwdDbl_, S_.tileLive);
                 CK(cudaGetLastError());
             }
@@ -1464,7 +1526,7 @@ private:
         const int lanes = kRedThreads / TB;
         const size_t sm = (size_t)nv_ * lanes * TB * sizeof(double);
         dim3 grid((unsigned)((B_ + TB - 1) / TB), (unsigned)chunks_);
-        k_reduce<T><<<grid, kRedThreads, sm, stream_>>>(D_, A);
+        withAnderson([&](auto mc) { k_reduce<T, decltype(mc)::value><<<grid, kRedThreads, sm, stream_>>>(D_, A); });
         CK(cudaGetLastError());
     }
 
@@ -1496,8 +1558,25 @@ private:
         }
         const long bx = (B_ + 255) / 256;  // about 8 blocks of 256 threads per SM
         const long by = std::max<long>(1, std::min<long>((152 * 8 + bx - 1) / bx, D_.sZ));
-        k_update<T><<<dim3((unsigned)bx, (unsigned)by), 256, 0, stream_>>>(D_, A);
+        withAnderson([&](auto mc) {
+            k_update<T, decltype(mc)::value><<<dim3((unsigned)bx, (unsigned)by), 256, 0, stream_>>>(D_, A);
+        });
         CK(cudaGetLastError());
+    }
+
+    // f(std::integral_constant<int, m>) for the solver's Anderson memory m (1 .. kMaxAnderson).
+    template <typename F>
+    void withAnderson(F f) const {
+        switch (opt_.anderson) {
+            case 1: f(std::integral_constant<int, 1>{}); break;
+            case 2: f(std::integral_constant<int, 2>{}); break;
+            case 3: f(std::integral_constant<int, 3>{}); break;
+            case 4: f(std::integral_constant<int, 4>{}); break;
+            case 5: f(std::integral_constant<int, 5>{}); break;
+            case 6: f(std::integral_constant<int, 6>{}); break;
+            case 7: f(std::integral_constant<int, 7>{}); break;
+            default: f(std::integral_constant<int, 8>{}); break;
+        }
     }
 
     void roundSpock() {

@@ -32,6 +32,7 @@ struct Dims {
     long sZ;
     int B;   // instances
     int TB;  // instances per CTA in the node kernels
+    int gmat;  // kernels that read their node matrices in place (kGmat* bits of kernels_batch.cuh)
 };
 
 template <typename T>

@@ -22,6 +22,9 @@ constexpr int kTileB = 32;     // instances per CTA (one per lane)
 constexpr int kTileWarps = 8;  // warps per CTA
 constexpr int kRT = 16;        // output rows per register block
 constexpr int kMaxTasks = 2;   // register blocks per warp: rows <= 16 * 8 * 2 = 256
+// Dims::gmat bits: the kernel reads its node matrices in place (global memory, through L1/L2)
+// instead of staging them in shared memory, for problems whose matrices exceed it.
+constexpr int kGmatLstar = 1, kGmatLop = 2, kGmatBack = 4, kGmatFwd = 8;
 
 __host__ __device__ inline int pad16(int r) { return (r + 15) & ~15; }
 
@@ -45,6 +48,8 @@ struct PadMats {
     const T *lSqrtQ, *lq;            // leaf cost
     const T *BTr, *APB, *ABKTr;      // per node (child j)
     const T *Kt, *K, *chol;          // per nonleaf node: K' (nx x nu), K (nu x nx), lower Cholesky (nu x nu)
+    const T *cholInv, *cholInvLo;    // per nonleaf node: (I + sum B'PB)^-1 (nu x nu) from the factor in FP64,
+                                     // as float hi + lo (FP32 solvers only)
     const T *AB;                     // per node: [A B] (nx x nxu)
     const T *nlG, *nlGT, *lG, *lGT;  // polyhedral constraints: Gamma and Gamma' (nonleaf, leaf)
 };
@@ -224,6 +229,40 @@ __device__ __forceinline__ void gemvc(T acc[kMaxTasks][kRT], T cmp[kMaxTasks][kR
     }
 }
 
+// One 16-row block `task` of a padded matrix: acc[t] += sum_k M[task*16 + t, k] * in(k).
+template <typename T, typename In>
+__device__ __forceinline__ void gemvTask(T acc[kRT], const T *M, int rows, int K, int task, In in) {
+    const int ld = pad16(rows);
+    const T *col = M + task * kRT;
+    int k = 0;
+    for (; k + 2 <= K; k += 2) {
+        T m0[kRT], m1[kRT];
+        load16(col + (size_t)k * ld, m0);
+        load16(col + (size_t)(k + 1) * ld, m1);
+        const T v0 = in(k), v1 = in(k + 1);
+        axpy16(acc, m0, v0);
+        axpy16(acc, m1, v1);
+    }
+    if (k < K) {
+        T m0[kRT];
+        load16(col + (size_t)k * ld, m0);
+        axpy16(acc, m0, in(k));
+    }
+}
+
+// The same with Dot2 accumulation (see gemvc).
+template <typename T, typename In>
+__device__ __forceinline__ void gemvcTask(T acc[kRT], T cmp[kRT], const T *M, int rows, int K, int task, In in) {
+    const int ld = pad16(rows);
+    const T *col = M + task * kRT;
+#pragma unroll 1
+    for (int k = 0; k < K; k++) {
+        T m0[kRT];
+        load16(col + (size_t)k * ld, m0);
+        axpy16c(acc, cmp, m0, in(k));
+    }
+}
+
 // Gather rows rowOf(0..n-1) of `src` for instances b0 .. b0+31 into sm[r*32 + lane].
 template <typename T, typename RowOf>
 __device__ __forceinline__ void gather(T *sm, int n, const T *src, int B, int b0, int lane, int warp, RowOf rowOf) {
@@ -237,7 +276,7 @@ __device__ __forceinline__ void gather(T *sm, int n, const T *src, int B, int b0
 //             leaf i:    [VI_l][V_l]
 // base rows,  nonleaf i: [x_i][u_i][y_i][t_ch][s_ch][t_0 s_0 at the root];  leaf: [x_i]
 // ------------------------------------------------------------------------------------------
-template <typename T, int MODE>
+template <typename T, int MODE, bool GM>
 __global__ void __launch_bounds__(kTileB *kTileWarps, kOpCtasPerSm<T>) k_lstar_b(const DevProblem<T> P, const Dims D, const OpArgs<T> A,
                                                                 const PadMats<T> M, int tilesPerCta, int dbl) {
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -295,15 +334,29 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, kOpCtasPerSm<T>) k_lstar_b
     const int perChild = linNl ? 0 : ldx * nx + ldu * nu + ldx + ldu;
     const int dG = nonleaf ? nxu : nx;  // Gamma' has dG rows (padded) and nG columns
     const int matG = nG ? pad16(dG) * nG : 0;
-    const int matElems = (nonleaf ? nc * perChild : (linL ? 0 : ldx * nx + ldx)) + matG;
+    // matrices staged in shared memory, or (GM: too large for it) read in place
+    constexpr bool gm = GM;
+    const int matElems = gm ? 0 : (nonleaf ? nc * perChild : (linL ? 0 : ldx * nx + ldx)) + matG;
     const int bufElems = (nIn * inArr + nBase * baseArr) * kTileB;  // one tile's input and base rows
-    T *sMat = sm, *sGT = sMat + matElems - matG, *sBuf = sMat + matElems;
+    T *sMat = sm, *sBuf = sMat + matElems;
+    const T *sGT = gm ? (nonleaf ? M.nlGT : M.lGT) : sMat + matElems - matG;
+    // child jj's [sqrtQ | sqrtR | q | r]: staged per child, or the per-node device arrays
+    auto mSqrtQ = [&](int jj) -> const T * { return gm ? M.sqrtQ + (size_t)(c0 + jj) * ldx * nx : sMat + jj * perChild; };
+    auto mSqrtR = [&](int jj) -> const T * {
+        return gm ? M.sqrtR + (size_t)(c0 + jj) * ldu * nu : sMat + jj * perChild + ldx * nx;
+    };
+    auto mQv = [&](int jj) -> const T * { return gm ? M.q + (size_t)(c0 + jj) * ldx : sMat + jj * perChild + ldx * nx + ldu * nu; };
+    auto mRv = [&](int jj) -> const T * {
+        return gm ? M.r + (size_t)(c0 + jj) * ldu : sMat + jj * perChild + ldx * nx + ldu * nu + ldx;
+    };
+    const T *mLeafQ = gm ? M.lSqrtQ : sMat, *mLeafq = gm ? M.lq : sMat + ldx * nx;
     T *sAv = sBuf + (dbl ? 2 : 1) * bufElems;  // the 4E+1 vector of the kernel projection
     // per-row extra terms of x_i / u_i (Gamma' times the Gamma rows, linear-cost gradients), dG x 32
     const bool extra = nG > 0 || (nonleaf ? linNl : linL);
     T *sGv = sAv + D.nd * kTileB;
-    if (nG) stageMat(sGT, nonleaf ? M.nlGT : M.lGT, matG);
-    if (nonleaf && !linNl) {
+    if (nG && !gm) stageMat(const_cast<T *>(sGT), nonleaf ? M.nlGT : M.lGT, matG);
+    if (gm) {
+    } else if (nonleaf && !linNl) {
         const bool qplNl = D.costNl == kCostQuadraticPlusLinear;
         for (int jj = 0; jj < nc; jj++) {
             const int j = c0 + jj;
@@ -418,13 +471,12 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, kOpCtasPerSm<T>) k_lstar_b
             const int sx = warp, su = slotFrom(warp, tasksOf(nx));  // x and u blocks on different warps
             for (int jj = 0; jj < nc && !linNl; jj++) {
                 const int r0 = jj * dIV;
-                const T *m = sMat + jj * perChild;
-                gemv(accX, m, nx, nx, sx, [&](int k) { return IN(r0 + k); });
-                gemv(accU, m + ldx * nx, nu, nu, su, [&](int k) { return IN(r0 + nx + k); });
+                gemv(accX, mSqrtQ(jj), nx, nx, sx, [&](int k) { return IN(r0 + k); });
+                gemv(accU, mSqrtR(jj), nu, nu, su, [&](int k) { return IN(r0 + nx + k); });
                 if (qpl) {
                     const T d23 = T(-0.5) * (IN(r0 + nxu) + IN(r0 + nxu + 1));
-                    gemv(accX, m + ldx * nx + ldu * nu, nx, 1, sx, [&](int) { return d23; });
-                    gemv(accU, m + ldx * nx + ldu * nu + ldx, nu, 1, su, [&](int) { return d23; });
+                    gemv(accX, mQv(jj), nx, 1, sx, [&](int) { return d23; });
+                    gemv(accU, mRv(jj), nu, 1, su, [&](int) { return d23; });
                 }
             }
     #pragma unroll
@@ -488,10 +540,10 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, kOpCtasPerSm<T>) k_lstar_b
             }
         } else {
             if (!linL) {
-                gemv(accX, sMat, nx, nx, warp, [&](int k) { return IN(k); });
+                gemv(accX, mLeafQ, nx, nx, warp, [&](int k) { return IN(k); });
                 if (D.costL == kCostQuadraticPlusLinear) {
                     const T d23 = T(-0.5) * (IN(nx) + IN(nx + 1));
-                    gemv(accX, sMat + ldx * nx, nx, 1, warp, [&](int) { return d23; });
+                    gemv(accX, mLeafq, nx, 1, warp, [&](int) { return d23; });
                 }
             }
     #pragma unroll
@@ -517,7 +569,7 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, kOpCtasPerSm<T>) k_lstar_b
 //             [y_j][s_j][x_j][u_j], leaf j: [x_j][s_j]
 // base rows:  nonleaf j: [I_j][II_j][III_j][IV_j];  leaf j: [IV_j][V_l][VI_l]
 // ------------------------------------------------------------------------------------------
-template <typename T, int MODE>
+template <typename T, int MODE, bool GM>
 __global__ void __launch_bounds__(kTileB *kTileWarps, kOpCtasPerSm<T>) k_lop_b(const DevProblem<T> P, const Dims D, const OpArgs<T> A,
                                                               const PadMats<T> M, int tilesPerCta, int dbl) {
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -579,16 +631,21 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, kOpCtasPerSm<T>) k_lop_b(c
     const int ldx = pad16(nx), ldu = pad16(nu);
     const int matIV = linNl ? 0 : ldx * nx + ldu * nu, matVI = (!nonleaf && !linL) ? ldx * nx : 0;
     const int matG = nG ? pad16(nG) * (nonleaf ? nxu : nx) : 0;  // Gamma, padded column-major
-    const int matElems = matIV + matVI + matG;
+    constexpr bool gm = GM;  // matrices read in place instead of staged
+    const int matElems = gm ? 0 : matIV + matVI + matG;
     const int bufElems = (nIn * inArr + nBase * baseArr) * kTileB;  // one tile's input and base rows
-    T *sMat = sm, *sw = sMat + matElems, *sPart = sw + dSoc * kTileB, *sBuf = sPart + kTileWarps * kTileB;
-    T *sG = sMat + matIV + matVI;
-    if (j > 0 && !linNl) {
-        stageMat(sMat, M.sqrtQ + (size_t)j * ldx * nx, ldx * nx);
-        stageMat(sMat + ldx * nx, M.sqrtR + (size_t)j * ldu * nu, ldu * nu);
+    T *sMatS = sm, *sw = sMatS + matElems, *sPart = sw + dSoc * kTileB, *sBuf = sPart + kTileWarps * kTileB;
+    if (!gm) {
+        if (j > 0 && !linNl) {
+            stageMat(sMatS, M.sqrtQ + (size_t)j * ldx * nx, ldx * nx);
+            stageMat(sMatS + ldx * nx, M.sqrtR + (size_t)j * ldu * nu, ldu * nu);
+        }
+        if (matVI) stageMat(sMatS + matIV, M.lSqrtQ, ldx * nx);
+        if (nG) stageMat(sMatS + matIV + matVI, nonleaf ? M.nlG : M.lG, matG);
     }
-    if (matVI) stageMat(sMat + matIV, M.lSqrtQ, ldx * nx);
-    if (nG) stageMat(sG, nonleaf ? M.nlG : M.lG, matG);
+    const T *sG = gm ? (nonleaf ? M.nlG : M.lG) : sMatS + matIV + matVI;
+    const T *mSqrtQ = gm ? M.sqrtQ + (size_t)j * ldx * nx : sMatS, *mSqrtR = gm ? M.sqrtR + (size_t)j * ldu * nu : sMatS + ldx * nx;
+    const T *mLeafQ = gm ? M.lSqrtQ : sMatS + matIV;
     // This CTA's instance tiles [t0, t1), double-buffered as in k_lstar_b.
     const int nTiles = (B + kTileB - 1) / kTileB;
     const int t0 = blockIdx.x * tilesPerCta, t1 = min(t0 + tilesPerCta, nTiles);
@@ -756,8 +813,8 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, kOpCtasPerSm<T>) k_lop_b(c
             T h = 0;
             const int sx = warp, su = slotFrom(warp, tasksOf(nx));  // x and u blocks on different warps
             if (j > 0) {
-                gemv(accX, sMat, nx, nx, sx, [&](int k) { return INP(k); });
-                gemv(accU, sMat + ldx * nx, nu, nu, su, [&](int k) { return INP(nx + k); });
+                gemv(accX, mSqrtQ, nx, nx, sx, [&](int k) { return INP(k); });
+                gemv(accU, mSqrtR, nu, nu, su, [&](int k) { return INP(nx + k); });
                 h = T(0.5) * INP(nxu);
                 if (D.costNl == kCostQuadraticPlusLinear) {
                     T lin = 0;
@@ -829,7 +886,7 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, kOpCtasPerSm<T>) k_lop_b(c
             }
             T accX[kMaxTasks][kRT];
             zeroAcc(accX);
-            gemv(accX, sMat + matIV, nx, nx, warp, [&](int k) { return INP(rx + k); });
+            gemv(accX, mLeafQ, nx, nx, warp, [&](int k) { return INP(rx + k); });
             T h = T(0.5) * INP(rs);
             if (D.costL == kCostQuadraticPlusLinear) {
                 T lin = 0;
@@ -877,8 +934,16 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, kOpCtasPerSm<T>) k_lop_b(c
 // inputs per instance tile: q of the children (-x of leaves at the last stage, else Q), u_i, x_i.
 // A CTA stages node i's matrices once and runs `tilesPerCta` instance tiles, double-buffered
 // when `dbl` (the rows of tile t + 1 load while tile t is computed).
+// Work split per tile, in three phases separated by barriers (U = 16-row blocks of u, X = of x):
+//  1. warps 0..U-1 form rhs = u_i - sum_j B_j' q_j, while the x blocks (on the warps after them,
+//     wrapping round) accumulate sum_j (A_j + B_j K_j)' P_j q_j, which does not depend on d;
+//  2. d = (I + sum B'PB)^-1 rhs: FP32 multiplies by the inverse, precomputed in FP64 from the
+//     cached Cholesky factor and kept as a float pair hi + lo, with Dot2 accumulation (so the
+//     solve is a product on U warps instead of a serial triangular solve on one, and is more
+//     accurate than a float triangular solve); FP64 keeps the reference's triangular solves;
+//  3. the x blocks add sum_j A_j'P_j B_j d + K_i'(d - u_i) and write q_i - x_i.
 // ------------------------------------------------------------------------------------------
-template <typename T>
+template <typename T, bool GM>
 __global__ void __launch_bounds__(kTileB *kTileWarps, 2) k_dyn_back_b(const DevProblem<T> P, const Dims D, const PadMats<T> M,
                                                                   const T *__restrict__ cand, T *__restrict__ Q,
                                                                   T *__restrict__ DD, int stageFrom, int stage,
@@ -891,20 +956,40 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, 2) k_dyn_back_b(const DevP
     const int c0 = P.chFrom[i], nc = P.numCh[i];
     const bool leafChildren = c0 >= D.nnl;
     const int ldx = pad16(nx), ldu = pad16(nu);
+    const int U = tasksOf(nu);
     const int perChild = ldu * nx + ldx * nu + ldx * nx;  // B', APB, (A+BK)'
     const int bufElems = (nc * nx + nu + nx) * kTileB;   // one tile's q, u and x rows
-    T *sMat = sm, *sKt = sMat + nc * perChild, *sL = sKt + ldx * nu, *sd = sL + ldu * nu, *sBuf = sd + nu * kTileB;
-    for (int jj = 0; jj < nc; jj++) {
-        const int j = c0 + jj;
-        T *m = sMat + jj * perChild;
-        stageMat(m, M.BTr + (size_t)j * ldu * nx, ldu * nx);
-        if (stage > 0) {
-            stageMat(m + ldu * nx, M.APB + (size_t)j * ldx * nu, ldx * nu);
-            stageMat(m + ldu * nx + ldx * nu, M.ABKTr + (size_t)j * ldx * nx, ldx * nx);
+    constexpr bool kInverse = sizeof(T) == 4;            // FP32: d by the inverse (phase 2)
+    constexpr bool gm = GM;  // matrices read in place instead of staged
+    const int matElems = gm ? 0 : nc * perChild + ldx * nu + ldu * nu;
+    // d: FP32 writes it next to rhs (into the tile's q rows, free after phase 1, when they are
+    // large enough: nx >= nu; else into a buffer of its own); FP64 solves in place
+    const bool dOwn = kInverse && nx < nu;
+    T *sMat = sm, *sd = sm + matElems, *sdOwn = sd + nu * kTileB, *sBuf = sdOwn + (dOwn ? nu * kTileB : 0);
+    T *sKtS = sMat + nc * perChild, *sLS = sKtS + ldx * nu;
+    const T *gL = (kInverse ? M.cholInv : M.chol) + (size_t)i * ldu * nu;
+    const T *sKt = gm ? M.Kt + (size_t)i * ldx * nu : sKtS, *sL = gm ? gL : sLS;
+    const T *sLlo = kInverse ? M.cholInvLo + (size_t)i * ldu * nu : nullptr;  // small: read in place
+    auto mBTr = [&](int jj) -> const T * { return gm ? M.BTr + (size_t)(c0 + jj) * ldu * nx : sMat + jj * perChild; };
+    auto mAPB = [&](int jj) -> const T * {
+        return gm ? M.APB + (size_t)(c0 + jj) * ldx * nu : sMat + jj * perChild + ldu * nx;
+    };
+    auto mABKTr = [&](int jj) -> const T * {
+        return gm ? M.ABKTr + (size_t)(c0 + jj) * ldx * nx : sMat + jj * perChild + ldu * nx + ldx * nu;
+    };
+    if (!gm) {
+        for (int jj = 0; jj < nc; jj++) {
+            const int j = c0 + jj;
+            T *m = sMat + jj * perChild;
+            stageMat(m, M.BTr + (size_t)j * ldu * nx, ldu * nx);
+            if (stage > 0) {
+                stageMat(m + ldu * nx, M.APB + (size_t)j * ldx * nu, ldx * nu);
+                stageMat(m + ldu * nx + ldx * nu, M.ABKTr + (size_t)j * ldx * nx, ldx * nx);
+            }
         }
+        if (stage > 0) stageMat(sKtS, M.Kt + (size_t)i * ldx * nu, ldx * nu);
+        stageMat(sLS, gL, ldu * nu);
     }
-    if (stage > 0) stageMat(sKt, M.Kt + (size_t)i * ldx * nu, ldx * nu);
-    stageMat(sL, M.chol + (size_t)i * ldu * nu, ldu * nu);
     const int nTiles = (B + kTileB - 1) / kTileB;
     const int t0 = blockIdx.x * tilesPerCta, t1 = min(t0 + tilesPerCta, nTiles);
     auto isLive = [&](int t) { return !live || live[t] != 0; };
@@ -926,6 +1011,7 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, 2) k_dyn_back_b(const DevP
     };
     if (t0 < t1) prefetch(t0);
     cpAsyncCommit();
+    const int sxw = slotFrom(warp, U);  // the x blocks start on the warp after the u blocks
     for (int tile = t0; tile < t1; tile++) {
         if (dbl && tile + 1 < t1) prefetch(tile + 1);
         cpAsyncCommit();
@@ -944,23 +1030,46 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, 2) k_dyn_back_b(const DevP
             }
             __syncthreads();
         }
-        T acc[kMaxTasks][kRT];
-        zeroAcc(acc);
-        for (int jj = 0; jj < nc; jj++) {
-            const T *qv = sq + jj * nx * kTileB + lane;
-            gemv(acc, sMat + jj * perChild, nu, nx, warp, [&](int k) { return qv[k * kTileB]; });
-        }
+        // phase 1
+        for (int task = warp; task < U; task += kTileWarps) {
+            T a[kRT];
 #pragma unroll
-        for (int q = 0; q < kMaxTasks; q++) {
-            const int r0 = (warp + q * kTileWarps) * kRT;
+            for (int t = 0; t < kRT; t++) a[t] = T(0);
+            for (int jj = 0; jj < nc; jj++) {
+                const T *qv = sq + jj * nx * kTileB + lane;
+                gemvTask(a, mBTr(jj), nu, nx, task, [&](int k) { return qv[k * kTileB]; });
+            }
 #pragma unroll
             for (int t = 0; t < kRT; t++) {
-                const int r = r0 + t;
-                if (r < nu) sd[r * kTileB + lane] = su[r * kTileB + lane] - acc[q][t];
+                const int r = task * kRT + t;
+                if (r < nu) sd[r * kTileB + lane] = su[r * kTileB + lane] - a[t];
             }
         }
+        T acc[kMaxTasks][kRT];
+        zeroAcc(acc);
+        if (stage > 0)
+            for (int jj = 0; jj < nc; jj++) {
+                const T *qv = sq + jj * nx * kTileB + lane;
+                gemv(acc, mABKTr(jj), nx, nx, sxw, [&](int k) { return qv[k * kTileB]; });
+            }
         __syncthreads();
-        if (warp == 0) {  // (I + sum B'PB) d = rhs with the cached lower Cholesky factor
+        // phase 2
+        T *sd2 = dOwn ? sdOwn : sq;
+        const T *dv = kInverse ? sd2 : sd;
+        if (kInverse) {
+            for (int task = warp; task < U; task += kTileWarps) {  // d = (Rinv_hi + Rinv_lo) rhs, Dot2
+                T a[kRT], cm[kRT];
+#pragma unroll
+                for (int t = 0; t < kRT; t++) a[t] = cm[t] = T(0);
+                gemvcTask(a, cm, sL, nu, nu, task, [&](int k) { return sd[k * kTileB + lane]; });
+                gemvTask(cm, sLlo, nu, nu, task, [&](int k) { return sd[k * kTileB + lane]; });
+#pragma unroll
+                for (int t = 0; t < kRT; t++) {
+                    const int r = task * kRT + t;
+                    if (r < nu) sd2[r * kTileB + lane] = finishc(a[t], cm[t], T(0));
+                }
+            }
+        } else if (warp == 0) {  // (I + sum B'PB) d = rhs with the cached lower Cholesky factor
             const T *L = sL;  // padded: L(r, k) at k * ldu + r
             T *v = sd + lane;
             for (int r = 0; r < nu; r++) {
@@ -976,20 +1085,16 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, 2) k_dyn_back_b(const DevP
         }
         __syncthreads();
         if (act)
-            for (int r = warp; r < nu; r += kTileWarps) DD[ix((long)i * nu + r, B, b)] = sd[r * kTileB + lane];
+            for (int r = warp; r < nu; r += kTileWarps) DD[ix((long)i * nu + r, B, b)] = dv[r * kTileB + lane];
+        // phase 3
         if (stage > 0) {
-            zeroAcc(acc);
-            for (int jj = 0; jj < nc; jj++) {
-                const T *m = sMat + jj * perChild;
-                const T *qv = sq + jj * nx * kTileB + lane;
-                gemv(acc, m + ldu * nx, nx, nu, warp, [&](int k) { return sd[k * kTileB + lane]; });
-                gemv(acc, m + ldu * nx + ldx * nu, nx, nx, warp, [&](int k) { return qv[k * kTileB]; });
-            }
-            gemv(acc, sKt, nx, nu, warp, [&](int k) { return sd[k * kTileB + lane] - su[k * kTileB + lane]; });
+            for (int jj = 0; jj < nc; jj++)
+                gemv(acc, mAPB(jj), nx, nu, sxw, [&](int k) { return dv[k * kTileB + lane]; });
+            gemv(acc, sKt, nx, nu, sxw, [&](int k) { return dv[k * kTileB + lane] - su[k * kTileB + lane]; });
             if (act) {
 #pragma unroll
                 for (int q = 0; q < kMaxTasks; q++) {
-                    const int r0 = (warp + q * kTileWarps) * kRT;
+                    const int r0 = (sxw + q * kTileWarps) * kRT;
 #pragma unroll
                     for (int t = 0; t < kRT; t++) {
                         const int r = r0 + t;
@@ -1012,8 +1117,12 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, 2) k_dyn_back_b(const DevP
 // stages deep, and plain float accumulation there leaves errors (~1e-6 relative) that change
 // from one T evaluation to the next and spoil the residual differences Anderson and the
 // SuperMann tests compare.
+// Work split per tile: the u blocks (U of them) go to warps 0..U-1; the children's x blocks
+// (X per child) are dealt to the register slots after them.  Children whose blocks fit in that
+// first deal accumulate A_j x while u is being formed, and add B_j u after the barrier; any
+// further children (wide trees with large states) follow one at a time.
 // ------------------------------------------------------------------------------------------
-template <typename T>
+template <typename T, bool GM>
 __global__ void __launch_bounds__(kTileB *kTileWarps, 2) k_dyn_fwd_b(const DevProblem<T> P, const Dims D, const PadMats<T> M,
                                                                  T *__restrict__ cand, const T *__restrict__ DD,
                                                                  const T *__restrict__ x0s, int stageFrom,
@@ -1026,11 +1135,18 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, 2) k_dyn_fwd_b(const DevPr
     const int nx = D.nx, nu = D.nu, nxu = D.nxu;
     const int c0 = P.chFrom[i], nc = P.numCh[i];
     const int ldx = pad16(nx), ldu = pad16(nu);
+    const int U = tasksOf(nu), X = tasksOf(nx);
+    // children overlapped with u (their blocks take the slots U .. U + G X - 1 of 8 kMaxTasks)
+    const int G = min(nc, max(0, (kTileWarps * kMaxTasks - U) / X));
     const int nZ = nu + nc * nx + (i == 0 ? nx : 0);      // Z of [u_i][x_children][x_0]
     const int bufElems = (nxu + nu + nZ) * kTileB;         // one tile's [x_i u_i], d_i and Z rows
-    T *sK = sm, *sAB = sK + ldu * nx, *sBuf = sAB + nc * ldx * nxu;
-    stageMat(sK, M.K + (size_t)i * ldu * nx, ldu * nx);
-    for (int jj = 0; jj < nc; jj++) stageMat(sAB + jj * ldx * nxu, M.AB + (size_t)(c0 + jj) * ldx * nxu, ldx * nxu);
+    constexpr bool gm = GM;  // matrices read in place instead of staged
+    T *sKS = sm, *sABS = sKS + ldu * nx, *sBuf = gm ? sm : sABS + nc * ldx * nxu;
+    const T *sK = gm ? M.K + (size_t)i * ldu * nx : sKS, *sAB = gm ? M.AB + (size_t)c0 * ldx * nxu : sABS;
+    if (!gm) {
+        stageMat(sKS, M.K + (size_t)i * ldu * nx, ldu * nx);
+        for (int jj = 0; jj < nc; jj++) stageMat(sABS + jj * ldx * nxu, M.AB + (size_t)(c0 + jj) * ldx * nxu, ldx * nxu);
+    }
     const int nTiles = (B + kTileB - 1) / kTileB;
     const int t0 = blockIdx.x * tilesPerCta, t1 = min(t0 + tilesPerCta, nTiles);
     auto isLive = [&](int t) { return !live || live[t] != 0; };
@@ -1073,29 +1189,65 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, 2) k_dyn_fwd_b(const DevPr
         T acc[kMaxTasks][kRT], cmp[kMaxTasks][kRT];  // Dot2 sums (gemvc): the rollout is compensated
         zeroAcc(acc);
         zeroAcc(cmp);
-        gemvc(acc, cmp, sK, nu, nx, warp, [&](int k) { return sxu[k * kTileB + lane]; });
+        // register slot q of this warp holds block (warp + 8 q) of the deal: u blocks first, then
+        // the overlapped children's x blocks
+        auto childOf = [&](int q, int &jj, int &task) {
+            const int ct = warp + q * kTileWarps - U;
+            if (ct < 0 || ct >= G * X) return false;
+            jj = ct / X;
+            task = ct % X;
+            return true;
+        };
+        // phase 1: u = K x + d on the u blocks' warps; A_j x of the overlapped children
 #pragma unroll
         for (int q = 0; q < kMaxTasks; q++) {
-            const int r0 = (warp + q * kTileWarps) * kRT;
+            const int blk = warp + q * kTileWarps;
+            if (blk < U) {
+                gemvcTask(acc[q], cmp[q], sK, nu, nx, blk, [&](int k) { return sxu[k * kTileB + lane]; });
+#pragma unroll
+                for (int t = 0; t < kRT; t++) {
+                    const int r = blk * kRT + t;
+                    if (r < nu) {
+                        const T u = finishc(acc[q][t], cmp[q][t], sdd[r * kTileB + lane]);
+                        sxu[(nx + r) * kTileB + lane] = u;
+                        if (act) {
+                            cand[ix((long)i * nu + r, B, b)] = u;
+                            if (R) R[ix((long)i * nu + r, B, b)] = sz[r * kTileB + lane] - u;
+                        }
+                    }
+                }
+                continue;
+            }
+            int jj, task;
+            if (childOf(q, jj, task))
+                gemvcTask(acc[q], cmp[q], sAB + jj * ldx * nxu, nx, nx, task, [&](int k) { return sxu[k * kTileB + lane]; });
+        }
+        __syncthreads();  // u is complete before the children read it
+        // phase 2: + B_j u, then x_j = (sum) + e_j for the overlapped children
+#pragma unroll
+        for (int q = 0; q < kMaxTasks; q++) {
+            int jj, task;
+            if (!childOf(q, jj, task)) continue;
+            gemvcTask(acc[q], cmp[q], sAB + jj * ldx * nxu + (size_t)nx * ldx, nx, nu, task,
+                      [&](int k) { return sxu[(nx + k) * kTileB + lane]; });
+            if (!act) continue;
+            const int j = c0 + jj;
 #pragma unroll
             for (int t = 0; t < kRT; t++) {
-                const int r = r0 + t;
-                if (r < nu) {
-                    const T u = finishc(acc[q][t], cmp[q][t], sdd[r * kTileB + lane]);
-                    sxu[(nx + r) * kTileB + lane] = u;
-                    if (act) {
-                        cand[ix((long)i * nu + r, B, b)] = u;
-                        if (R) R[ix((long)i * nu + r, B, b)] = sz[r * kTileB + lane] - u;
-                    }
+                const int r = task * kRT + t;
+                if (r < nx) {
+                    const T x = finishc(acc[q][t], cmp[q][t], D.affine ? P.e[(size_t)j * nx + r] : T(0));
+                    cand[ix(D.oX + (long)j * nx + r, B, b)] = x;
+                    if (R) R[ix(D.oX + (long)j * nx + r, B, b)] = sz[(nu + jj * nx + r) * kTileB + lane] - x;
                 }
             }
         }
-        __syncthreads();  // u is complete before the children read [x; u]
-        for (int jj = 0; jj < nc; jj++) {
+        // the remaining children, one at a time over all warps
+        for (int jj = G; jj < nc; jj++) {
             const int j = c0 + jj;
             zeroAcc(acc);
             zeroAcc(cmp);
-            const int slot = slotFrom(warp, jj * tasksOf(nx));  // children's blocks on different warps
+            const int slot = slotFrom(warp, jj * X);  // children's blocks on different warps
             gemvc(acc, cmp, sAB + jj * ldx * nxu, nx, nxu, slot, [&](int k) { return sxu[k * kTileB + lane]; });
             if (!act) continue;
 #pragma unroll
@@ -1126,16 +1278,17 @@ namespace spock {
 // Host-side launchers of the two largest kernels.  Each (kernel, precision, mode) is compiled in
 // a translation unit of its own (ops_batch.cu, built once per combination), so their device
 // code compiles in parallel; the engine calls these instead of launching the kernels itself.
-template <typename T, int MODE>
+// GM: the variant that reads node matrices in place (problems whose matrices exceed shared memory).
+template <typename T, int MODE, bool GM>
 void launchLstarB(dim3 grid, size_t smem, cudaStream_t stream, const DevProblem<T> &P, const Dims &D, const OpArgs<T> &A,
                   const PadMats<T> &M, int tilesPerCta, int dbl);
-template <typename T, int MODE>
+template <typename T, int MODE, bool GM>
 void launchLopB(dim3 grid, size_t smem, cudaStream_t stream, const DevProblem<T> &P, const Dims &D, const OpArgs<T> &A,
                 const PadMats<T> &M, int tilesPerCta, int dbl);
 // cudaFuncSetAttribute(MaxDynamicSharedMemorySize) of the same kernels.
-template <typename T, int MODE>
+template <typename T, int MODE, bool GM>
 cudaError_t optInLstarB(int bytes);
-template <typename T, int MODE>
+template <typename T, int MODE, bool GM>
 cudaError_t optInLopB(int bytes);
 
 }  // namespace spock

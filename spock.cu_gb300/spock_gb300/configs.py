@@ -82,9 +82,11 @@ def config2(path, seed=0, count=1, nx=50, nu=20, horizon=10, stopping=4, states=
     return path, rng.uniform(-1., 1., size=(count, nx))
 
 
-def config3(path, seed=0, count=1, nx=100, nu=40, horizon=8, stopping=3, events=5, radius=2.):
+def config3(path, seed=0, count=1, nx=100, nu=40, horizon=8, stopping=3, events=5, radius=2., ball=True):
     """Box |x| <= 3 on the states and the input ball ||u||_2 <= 2 (RectangleInputBall); the ball
-    needs equal input scales, so this problem is not preconditioned."""
+    needs equal input scales, so this problem is not preconditioned.  With ball=False the input
+    constraint is the box |u_i| <= radius instead (Rectangle, preconditioned): the variant the
+    reference's constraint types can express."""
     rng = np.random.default_rng(seed)
     tree = F.IidProcess(np.ones(events) / events, horizon=horizon, stopping_stage=stopping).build()
     dyn = _stable_dynamics(rng, nx, nu, events)
@@ -94,10 +96,12 @@ def config3(path, seed=0, count=1, nx=100, nu=40, horizon=8, stopping=3, events=
     (F.Factory(tree, nx, nu).with_dynamics_events(dyn)
      .with_cost_nonleaf_events(costs)
      .with_cost_leaf(leaf)
-     .with_constraint_nonleaf(F.RectangleInputBall(-3. * np.ones(nx), 3. * np.ones(nx), nu, radius))
+     .with_constraint_nonleaf(F.RectangleInputBall(-3. * np.ones(nx), 3. * np.ones(nx), nu, radius) if ball else
+                              F.Rectangle(np.concatenate((-3. * np.ones(nx), -radius * np.ones(nu))),
+                                          np.concatenate((3. * np.ones(nx), radius * np.ones(nu)))))
      .with_constraint_leaf(F.Rectangle(-3. * np.ones(nx), 3. * np.ones(nx)))
      .with_risk(F.AVaR(.9))
-     .with_preconditioning(False)
+     .with_preconditioning(not ball)
      .generate_problem(path))
     return path, rng.uniform(-1., 1., size=(count, nx))
 
