@@ -138,6 +138,10 @@ int spock_op(spock_solver s, const double *prim, double *dual);            /* Li
 int spock_adj(spock_solver s, const double *dual, double *prim);           /* LinearOperator::adj (operator.cuh:62-82) */
 int spock_cp_step(spock_solver s, const double *x0, const double *z, double *cand); /* Cache::iter (cache.cuh:795-801) */
 int spock_apply_m(spock_solver s, const double *z, double *mz);            /* M of Cache::dotM (cache.cuh:721-734) */
+/* Cache::getDual (cache.cuh:371-376): the dual candidate prox_{g*}(z_d + gamma L(2 prim - z_p))
+ * for a given primal candidate `prim` (sizePrimal values) at the solver's current iterate z
+ * (instance 0; for a batch, every instance gets `prim`); `dual` receives sizeDual values. */
+int spock_get_dual(spock_solver s, const double *prim, double *dual);
 
 /* Measurement hooks for the benchmark: CUDA-event time of one launch of a named kernel
  * ("lstar", "lop", "mlstar", "mlop", "dyn", "reduce", "update", "teval", "round"), its
@@ -180,6 +184,19 @@ int spock_set_tuning(spock_solver s, const int *in3);
  * device), so make that first call before any stream capture.  All calls share the one buffer: calls that
  * overlap on the GPU (other threads, other streams) race with each other. */
 int spock_project_dynamics_noalloc(spock_solver s, const void *x0, void *prim_ux, void *stream);
+
+/* ---- Tensor-core GEMM and the learned warm start's reconstruction (no reference counterpart).
+ * spock_gemm_bf16: D = alpha A B' (+ rowAdd[m]) (+ colAdd[n]) on the tcgen05 tensor cores, A
+ * (M x K) and B (N x K) BF16 device arrays, row-major with K contiguous, K a multiple of 64,
+ * FP32 accumulation; D (FP32 row-major M x N, leading dimension ldd) gets the sum and Dact its
+ * GELU (tanh form) when gelu is nonzero; either may be NULL.  Synchronous on `device`.
+ * spock_warm_start_pca: sets an FP32 solver's iterate to mean + basis coef' (basis: sizeIterate x
+ * k, coef: batch x k, BF16 row-major, k a multiple of 64; mean: sizeIterate FP32 values, all
+ * device arrays) with the same GEMM writing the solver's element-major iterate directly; then
+ * re-solve with spock_resolve. */
+int spock_gemm_bf16(const void *A, const void *B, long M, long N, int K, float alpha, const float *rowAdd,
+                    const float *colAdd, int gelu, float *D, float *Dact, long ldd, int device);
+int spock_warm_start_pca(spock_solver s, const void *basis, const void *coef, int k, const float *mean);
 
 /* ---- Learned warm start (no reference counterpart).  A three-layer MLP x0 -> coefficients of a
  * solution basis, trained and evaluated by the library's own kernels: dims4 = {inputs, hidden,

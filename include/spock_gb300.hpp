@@ -160,6 +160,14 @@ class Cache {
         std::vector<T> z = solution(instance);
         return std::vector<T>(z.begin() + (long)sizePrimal(), z.end());
     }
+    // Cache::getDual (cache.cuh:371-376): the dual candidate for a given primal candidate at the
+    // current iterate (a copy instead of a device tensor).
+    std::vector<T> getDual(const std::vector<T> &primal) const {
+        if ((long)primal.size() != (long)sizePrimal()) throw std::invalid_argument("[getDual] primal has the wrong size");
+        std::vector<double> p(primal.begin(), primal.end()), d(sizeDual());
+        check(spock_get_dual(h_.get(), p.data(), d.data()));
+        return std::vector<T>(d.begin(), d.end());
+    }
     // Cache::states()/inputs() (cache.cuh:386-412), unscaled.
     std::vector<T> states(long instance = 0) const {
         std::vector<double> xs(tree_.numStates() * tree_.numNodes());
@@ -220,7 +228,7 @@ class CacheBuilder {
     CacheBuilder &andersonBuffer(size_t m) { o_.anderson = (long)m; return *this; }
     // The reference's debug mode caps the iterations at 1000 when none are set (cache.cuh:1204-1208)
     // and records error histories; only the cap is kept here.
-    CacheBuilder &enableDebug(bool enable) {
+    CacheBuilder &enableDebug(bool enable = true) {
         if (enable && o_.max_iters == 0) o_.max_iters = 1000;
         return *this;
     }

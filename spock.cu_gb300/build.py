@@ -14,7 +14,7 @@ SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libspock_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["engine.cu", "problem.cpp", "capi.cpp", "noalloc.cu", "offline.cu", "mlp.cu", "ops_batch.cu"]
+SOURCES = ["engine.cu", "problem.cpp", "capi.cpp", "noalloc.cu", "offline.cu", "mlp.cu", "umma_gemm.cu", "ops_batch.cu"]
 # ops_batch.cu is compiled once per batched operator kernel, precision, mode and matrix placement
 OPS_VARIANTS = [(k, t, m, g) for k in ("LSTAR", "LOP") for t in ("float", "double") for m in (0, 1, 2) for g in (0, 1)]
 

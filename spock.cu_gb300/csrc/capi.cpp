@@ -373,6 +373,15 @@ int spock_cp_step(spock_solver sv, const double *x0, const double *z, double *ca
     });
 }
 
+int spock_get_dual(spock_solver sv, const double *prim, double *dual) {
+    return guard([&] {
+        auto *s = solver(sv);
+        need(prim, "prim");
+        need(dual, "dual");
+        s->eng->dualOf(prim, dual);
+    });
+}
+
 int spock_apply_m(spock_solver sv, const double *z, double *mz) {
     return guard([&] {
         auto *s = solver(sv);

@@ -23,6 +23,7 @@
 
 #include "engine.cuh"
 #include "kernels.cuh"
+#include "umma_gemm.hpp"
 #include "kernels_batch.cuh"
 
 namespace spock {
@@ -105,22 +106,35 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce(const Dims Dm, const Red
             T blk[NV];
 #pragma unroll
             for (int v = 0; v < NV; v++) blk[v] = 0;
-#pragma unroll 4
-            for (long k = kb; k < ke; k += lanes) {
-                const size_t o = ix(k, B, b);
-                const T r = A.R[o], mr = A.MR[o];
-                blk[0] += r * mr;
-                amax = fmax(amax, fabs(mr));
-                if (wantB) blk[2] += mr * A.D[o];
-                if (wantA) {
-                    const T c = r - A.RPREV[o];
+            // kU rows per step: every load of the step is issued (predicated on the phase, no
+            // branch) before any of its products, so kU x (3 + M) loads per thread are in flight
+            constexpr int kU = 4;
+            for (long k = kb; k < ke; k += (long)kU * lanes) {
+                T r[kU], mr[kU], rp[kU], dd[kU], an[M][kU];
+#pragma unroll
+                for (int q = 0; q < kU; q++) {
+                    const long kk = k + (long)q * lanes;
+                    const bool ok = kk < ke;
+                    const size_t o = ix(ok ? kk : k, B, b);
+                    r[q] = ok ? A.R[o] : T(0);
+                    mr[q] = ok ? A.MR[o] : T(0);
+                    dd[q] = ok && wantB ? A.D[o] : T(0);
+                    rp[q] = ok && wantA ? A.RPREV[o] : T(0);
+#pragma unroll
+                    for (int s = 0; s < M; s++) an[s][q] = ok && wantA ? A.ANDR[s * slot + o] : T(0);
+                }
+#pragma unroll
+                for (int q = 0; q < kU; q++) {
+                    blk[0] += r[q] * mr[q];
+                    amax = fmax(amax, fabs(mr[q]));
+                    blk[2] += mr[q] * dd[q];
+                    const T c = wantA ? r[q] - rp[q] : T(0);
                     blk[3] += c * c;
-                    blk[4] += c * r;
+                    blk[4] += c * r[q];
 #pragma unroll
                     for (int s = 0; s < M; s++) {
-                        const T a = A.ANDR[s * slot + o];
-                        blk[kNV0 + s] += c * a;
-                        blk[kNV0 + M + s] += a * r;
+                        blk[kNV0 + s] += c * an[s][q];
+                        blk[kNV0 + M + s] += an[s][q] * r[q];
                     }
                 }
             }
@@ -795,6 +809,32 @@ public:
         downloadSlice(CAND_, cand, 0, D_.sZ);
     }
 
+    // Cache::getDual (cache.cuh:371-376): the dual half of T at the current iterate with the given
+    // primal candidate, prox_{g*}(z_d + gamma L(2 prim - z_p)) (T form of L with CAND = prim).
+    void dualOf(const double *prim, double *dual) override {
+        allLive();
+        uploadSlice(CAND_, prim, 0, D_.sPrim);
+        launchLop<0>(tevalLopArgs());
+        downloadSlice(CAND_, dual, D_.sPrim, D_.sDual);
+    }
+
+    void warmStartPca(const void *basis, const void *coef, int k, const float *mean) override {
+        if (sizeof(T) != 4) throw std::invalid_argument("[warmStart] the PCA warm start writes FP32 solvers");
+        if (!basis || !coef || !mean) throw std::invalid_argument("[warmStart] null device pointer");
+        if (!gemmErr_) gemmErr_ = dalloc<int>(1);
+        CK(cudaMemsetAsync(gemmErr_, 0, sizeof(int), stream_));
+        GemmEpilogue E;
+        E.rowAdd = mean;
+        E.D = reinterpret_cast<float *>(Z_);  // element-major sZ x B = row-major with ldd = B
+        E.ldd = B_;
+        E.err = gemmErr_;
+        gemmBf16(basis, coef, D_.sZ, B_, k, E, stream_);
+        int err = 0;
+        CK(cudaMemcpyAsync(&err, gemmErr_, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+        if (err) throw std::runtime_error("[warmStart] the tensor-core pipeline gave up (code " + std::to_string(err) + ")");
+    }
+
     void applyM(const double *z, double *mz) override {
         allLive();
         // M z through the residual kernels, which read the residual buffer
@@ -989,6 +1029,7 @@ private:
     long capacity_ = 0;  // slots in live tiles after the last compaction
     int compactions_ = 0;
     double *part_ = nullptr;
+    int *gemmErr_ = nullptr;  // error flag of the tensor-core GEMM (warmStartPca)
     int *hostActive_ = nullptr, *devActive_ = nullptr;
     int chunks_ = 1, nv_ = 0;
     long rowsPerChunk_ = 1;

@@ -97,6 +97,10 @@ public:
     virtual void adj(const double *dual, double *prim) = 0;
     virtual void cpStep(const double *x0, const double *z, double *cand) = 0;
     virtual void applyM(const double *z, double *mz) = 0;
+    virtual void dualOf(const double *prim, double *dual) = 0;
+    // Learned warm start: iterate = mean + basis coef' on the device (FP32 solvers), where basis
+    // is sZ x k and coef batch x k, BF16 row-major, k a multiple of 64 (tcgen05 GEMM).
+    virtual void warmStartPca(const void *basis, const void *coef, int k, const float *mean) = 0;
     virtual int precisionBits() const = 0;
     // The current iterate on the device (sZ x batch, element-major, in the solver precision), and
     // its replacement by another solver's iterate of the same problem size and batch, converted

@@ -2,8 +2,10 @@
 //
 // The network maps an initial state x0 (nIn values) to the coefficients of a solution basis:
 //   A1 = W1 X + b1, H1 = gelu(A1);  A2 = W2 H1 + b2, H2 = gelu(A2);  Y = W3 H2 + b3,
-// columns = samples.  Weights live as FP32 master copies (for Adam) and BF16 copies that the
-// forward products read; every product accumulates in FP32.  GELU is the tanh form
+// columns = samples.  Weights live as FP32 master copies (for Adam) and BF16 copies that every
+// product reads; all products (forward, and both gradient products of the backward pass) run on
+// the tcgen05 tensor cores (umma_gemm.cu) with FP32 accumulation, activations and gradients
+// entering as hi + lo BF16 pairs.  GELU is the tanh form
 // 0.5 a (1 + tanh(sqrt(2/pi) (a + 0.044715 a^3))).
 //
 // C-ABI (spock_gb300.h): spock_mlp_create / _free / _set_params / _get_params / _forward /
@@ -19,6 +21,7 @@
 
 #include "../../include/spock_gb300.h"
 #include "capi_internal.hpp"
+#include "umma_gemm.hpp"
 
 namespace spock {
 
@@ -32,77 +35,12 @@ namespace {
                                      __FILE__ + ":" + std::to_string(__LINE__));                   \
     } while (0)
 
-__device__ __forceinline__ float ld(const float *p, size_t i) { return p[i]; }
-__device__ __forceinline__ float ld(const __nv_bfloat16 *p, size_t i) { return __bfloat162float(p[i]); }
-
-// C[m x n] = alpha * op(A)[m x k] op(B)[k x n] + beta * C, column-major with leading dimensions;
-// op transposes when tA / tB.  64 x 64 tiles, 256 threads with 4 x 4 outputs each, operands
-// staged through shared memory in 16-wide slabs, FP32 accumulation.
-constexpr int kBM = 64, kBN = 64, kBK = 16;
-
-template <typename TA, typename TB>
-__global__ void __launch_bounds__(256) k_gemm(int m, int n, int k, float alpha, const TA *A, int lda, bool tA,
-                                              const TB *B, int ldb, bool tB, float beta, float *C, int ldc) {
-    __shared__ float sA[kBK][kBM + 4];
-    __shared__ float sB[kBK][kBN + 4];
-    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-    const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * kBN;
-    float acc[4][4] = {};
-    for (int k0 = 0; k0 < k; k0 += kBK) {
-        for (int e = threadIdx.x; e < kBK * kBM; e += 256) {  // sA[kk][i] = op(A)(m0 + i, k0 + kk)
-            const int kk = e / kBM, i = e % kBM, r = m0 + i, c = k0 + kk;
-            float v = 0.f;
-            if (r < m && c < k) v = tA ? ld(A, (size_t)r * lda + c) : ld(A, (size_t)c * lda + r);
-            sA[kk][i] = v;
-        }
-        for (int e = threadIdx.x; e < kBK * kBN; e += 256) {  // sB[kk][j] = op(B)(k0 + kk, n0 + j)
-            const int kk = e / kBN, j = e % kBN, r = k0 + kk, c = n0 + j;
-            float v = 0.f;
-            if (r < k && c < n) v = tB ? ld(B, (size_t)r * ldb + c) : ld(B, (size_t)c * ldb + r);
-            sB[kk][j] = v;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int kk = 0; kk < kBK; kk++) {
-            float a[4], bv[4];
-#pragma unroll
-            for (int q = 0; q < 4; q++) a[q] = sA[kk][ty * 4 + q];
-#pragma unroll
-            for (int q = 0; q < 4; q++) bv[q] = sB[kk][tx * 4 + q];
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-#pragma unroll
-                for (int j = 0; j < 4; j++) acc[i][j] = fmaf(a[i], bv[j], acc[i][j]);
-        }
-        __syncthreads();
-    }
-#pragma unroll
-    for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const int r = m0 + ty * 4 + i, c = n0 + tx * 4 + j;
-            if (r < m && c < n) {
-                float *o = C + (size_t)c * ldc + r;
-                *o = alpha * acc[i][j] + (beta != 0.f ? beta * *o : 0.f);
-            }
-        }
-}
 
 __device__ __forceinline__ float geluTanh(float a, float *dgelu) {
     const float c = 0.7978845608028654f, u = c * (a + 0.044715f * a * a * a);
     const float t = tanhf(u);
     if (dgelu) *dgelu = 0.5f * (1.f + t) + 0.5f * a * (1.f - t * t) * c * (1.f + 3.f * 0.044715f * a * a);
     return 0.5f * a * (1.f + t);
-}
-
-// A += b (per row); H = gelu(A) when act, else H = A.
-__global__ void k_bias_act(float *A, float *H, const float *bias, int rows, int cols, int act) {
-    const size_t n = (size_t)rows * cols;
-    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
-        const float a = A[e] + bias[e % rows];
-        A[e] = a;
-        H[e] = act ? geluTanh(a, nullptr) : a;
-    }
 }
 
 // dA = dH * gelu'(A), in place on dH.
@@ -137,7 +75,7 @@ __global__ void k_rowsum(const float *dA, float *db, int rows, int cols) {
 }
 
 // Adam on FP32 master weights; refreshes the BF16 copy.
-__global__ void k_adam(float *w, __nv_bfloat16 *wb, const float *g, float *mo, float *v, size_t n, float lr, float b1,
+__global__ void k_adam(float *w, const float *g, float *mo, float *v, size_t n, float lr, float b1,
                        float b2, float eps, float c1, float c2) {
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
         const float gg = g[e];
@@ -146,42 +84,89 @@ __global__ void k_adam(float *w, __nv_bfloat16 *wb, const float *g, float *mo, f
         v[e] = v1;
         const float nw = w[e] - lr * (m1 / c1) / (sqrtf(v1 / c2) + eps);
         w[e] = nw;
-        if (wb) wb[e] = __float2bfloat16(nw);
     }
-}
-
-__global__ void k_to_bf16(const float *w, __nv_bfloat16 *wb, size_t n) {
-    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
-        wb[e] = __float2bfloat16(w[e]);
 }
 
 int grid1(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 8); }
 
-template <typename TA, typename TB>
-void gemm(cudaStream_t st, int m, int n, int k, float alpha, const TA *A, int lda, bool tA, const TB *B, int ldb,
-          bool tB, float beta, float *C, int ldc) {
-    dim3 g((unsigned)((m + kBM - 1) / kBM), (unsigned)((n + kBN - 1) / kBN));
-    k_gemm<TA, TB><<<g, 256, 0, st>>>(m, n, k, alpha, A, lda, tA, B, ldb, tB, beta, C, ldc);
-    MCK(cudaGetLastError());
+// BF16 operand copies for the tensor-core GEMMs (umma_gemm.cu: D = A B', both K-major).  An
+// FP32 matrix is split into hi = bf16(x) and lo = bf16(x - hi), which together carry about 16
+// bits of mantissa; the K dimension of an operand is then a concatenation of segments of 64-
+// padded length, each hi or lo, so one GEMM sums hi*hi + lo*hi (+ hi*lo) products: the weights
+// (BF16 by design) meet activations and gradients at close to FP32 accuracy.
+// Segment j of an operand row is lo when bit j of `loMask` is set, hi otherwise.
+
+// Rows: src (rows x d, row-major, FP32) -> dst (rows x nseg*dP, BF16), zero past column d.
+__global__ void k_split_rows(const float *src, int rows, int d, __nv_bfloat16 *dst, int dP, int nseg, int loMask) {
+    const size_t n = (size_t)rows * dP;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        const int r = (int)(e / dP), c = (int)(e % dP);
+        const float x = c < d ? src[(size_t)r * d + c] : 0.f;
+        const __nv_bfloat16 hi = __float2bfloat16_rn(x), lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+        for (int j = 0; j < nseg; j++) dst[(size_t)r * nseg * dP + (size_t)j * dP + c] = (loMask >> j) & 1 ? lo : hi;
+    }
 }
+
+// Transposed: src (rows x d, row-major, FP32) -> dst (d x nseg*rP, BF16), dst[c][j*rP + r] the
+// hi or lo part of src[r][c], zero for r >= rows.  32 x 32 tiles through shared memory.
+__global__ void k_split_cols(const float *src, int rows, int d, __nv_bfloat16 *dst, int rP, int nseg, int loMask) {
+    __shared__ float t[32][33];
+    const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32, tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int k = ty; k < 32; k += 8) {
+        const int r = r0 + k, c = c0 + tx;
+        t[k][tx] = (r < rows && c < d) ? src[(size_t)r * d + c] : 0.f;
+    }
+    __syncthreads();
+    for (int k = ty; k < 32; k += 8) {
+        const int c = c0 + k, r = r0 + tx;
+        if (c >= d || r >= rP) continue;
+        const float x = t[tx][k];
+        const __nv_bfloat16 hi = __float2bfloat16_rn(x), lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+        for (int j = 0; j < nseg; j++) dst[(size_t)c * nseg * rP + (size_t)j * rP + r] = (loMask >> j) & 1 ? lo : hi;
+    }
+}
+
+// The weights' BF16 operands from the FP32 master W (out x in, column-major):
+//   row form  (forward, B of X W'):      wr[o][j*inP + i] = bf16(W[o][i]), two equal segments;
+//   column form (backward, B of dA W):   wc[i][j*outP + o] = bf16(W[o][i]), two equal segments.
+__global__ void k_weight_ops(const float *W, int out, int in, __nv_bfloat16 *wr, int inP, __nv_bfloat16 *wc, int outP) {
+    const size_t n = (size_t)out * in;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        const int o = (int)(e % out), i = (int)(e / out);
+        const __nv_bfloat16 v = __float2bfloat16_rn(W[e]);
+        for (int j = 0; j < 2; j++) {
+            wr[(size_t)o * 2 * inP + (size_t)j * inP + i] = v;
+            if (wc) wc[(size_t)i * 2 * outP + (size_t)j * outP + o] = v;
+        }
+    }
+}
+
+inline int pad64(int v) { return (v + 63) & ~63; }
 
 }  // namespace
 
+
 // Three layers: sizes d0 -> d1 -> d2 -> d3.  Parameters packed as W1 (d1 x d0), b1, W2 (d2 x d1),
-// b2, W3 (d3 x d2), b3 in one FP32 array (and a BF16 copy of the W's at the same offsets).
+// b2, W3 (d3 x d2), b3 in one FP32 array (column-major W's: the Adam master copy).  Every product
+// runs on the tensor cores (gemmBf16): samples are rows (an activation "d x cols, column-major"
+// is "cols x d, row-major"), weights enter as BF16, activations and gradients as hi + lo BF16
+// pairs, accumulation in FP32.
 struct Mlp {
-    int d[4];
+    int d[4], dP[4];
     size_t off[6], total;
     float *w = nullptr, *g = nullptr, *mo = nullptr, *v = nullptr;
-    __nv_bfloat16 *wb = nullptr;
-    int cap = 0;  // columns the activations are allocated for
+    __nv_bfloat16 *wr[3] = {}, *wc[3] = {};  // weight operands (row and column forms)
+    int cap = 0;                              // columns the activations are allocated for
     float *A1 = nullptr, *H1 = nullptr, *A2 = nullptr, *H2 = nullptr, *Y = nullptr, *dY = nullptr, *dH = nullptr,
           *loss = nullptr;
+    __nv_bfloat16 *opA = nullptr, *opB = nullptr;  // activation / gradient operands
+    int *err = nullptr;
     long steps = 0;
     cudaStream_t st = nullptr;
 
     Mlp(int d0, int d1, int d2, int d3) {
         d[0] = d0; d[1] = d1; d[2] = d2; d[3] = d3;
+        for (int q = 0; q < 4; q++) dP[q] = pad64(d[q]);
         size_t o = 0;
         for (int l = 0; l < 3; l++) {
             off[2 * l] = o;
@@ -195,18 +180,33 @@ struct Mlp {
             MCK(cudaMalloc(p, sizeof(float) * total));
             MCK(cudaMemset(*p, 0, sizeof(float) * total));
         }
-        MCK(cudaMalloc(&wb, sizeof(__nv_bfloat16) * total));
+        for (int l = 0; l < 3; l++) {
+            MCK(cudaMalloc(&wr[l], sizeof(__nv_bfloat16) * (size_t)d[l + 1] * 2 * dP[l]));
+            MCK(cudaMemset(wr[l], 0, sizeof(__nv_bfloat16) * (size_t)d[l + 1] * 2 * dP[l]));
+            if (l > 0) {
+                MCK(cudaMalloc(&wc[l], sizeof(__nv_bfloat16) * (size_t)d[l] * 2 * dP[l + 1]));
+                MCK(cudaMemset(wc[l], 0, sizeof(__nv_bfloat16) * (size_t)d[l] * 2 * dP[l + 1]));
+            }
+        }
         MCK(cudaMalloc(&loss, sizeof(float)));
+        MCK(cudaMalloc(&err, sizeof(int)));
+        MCK(cudaMemset(err, 0, sizeof(int)));
     }
     ~Mlp() {
-        for (void *p : {(void *)w, (void *)g, (void *)mo, (void *)v, (void *)wb, (void *)A1, (void *)H1, (void *)A2,
-                        (void *)H2, (void *)Y, (void *)dY, (void *)dH, (void *)loss})
+        for (void *p : {(void *)w, (void *)g, (void *)mo, (void *)v, (void *)A1, (void *)H1, (void *)A2, (void *)H2,
+                        (void *)Y, (void *)dY, (void *)dH, (void *)loss, (void *)opA, (void *)opB, (void *)err})
             cudaFree(p);
+        for (int l = 0; l < 3; l++) {
+            cudaFree(wr[l]);
+            cudaFree(wc[l]);
+        }
         if (st) cudaStreamDestroy(st);
     }
     void reserve(int cols) {
         if (cols <= cap) return;
-        for (void *p : {(void *)A1, (void *)H1, (void *)A2, (void *)H2, (void *)Y, (void *)dY, (void *)dH}) cudaFree(p);
+        for (void *p : {(void *)A1, (void *)H1, (void *)A2, (void *)H2, (void *)Y, (void *)dY, (void *)dH, (void *)opA,
+                        (void *)opB})
+            cudaFree(p);
         const int wmax = std::max(d[1], d[2]);
         MCK(cudaMalloc(&A1, sizeof(float) * (size_t)d[1] * cols));
         MCK(cudaMalloc(&H1, sizeof(float) * (size_t)d[1] * cols));
@@ -215,48 +215,103 @@ struct Mlp {
         MCK(cudaMalloc(&Y, sizeof(float) * (size_t)d[3] * cols));
         MCK(cudaMalloc(&dY, sizeof(float) * (size_t)d[3] * cols));
         MCK(cudaMalloc(&dH, sizeof(float) * (size_t)wmax * cols));
+        // operands: rows x 2 dP (forward / backward data) or d x 3 colsP (weight gradients)
+        size_t ops = 0;
+        for (int q = 0; q < 4; q++) ops = std::max({ops, (size_t)cols * 2 * dP[q], (size_t)d[q] * 3 * pad64(cols)});
+        MCK(cudaMalloc(&opA, sizeof(__nv_bfloat16) * ops));
+        MCK(cudaMalloc(&opB, sizeof(__nv_bfloat16) * ops));
         cap = cols;
     }
     void refreshBf16() {
-        k_to_bf16<<<grid1(total), 256, 0, st>>>(w, wb, total);
+        for (int l = 0; l < 3; l++) {
+            k_weight_ops<<<grid1((size_t)d[l + 1] * d[l]), 256, 0, st>>>(w + off[2 * l], d[l + 1], d[l], wr[l], dP[l], wc[l],
+                                                                        dP[l + 1]);
+            MCK(cudaGetLastError());
+        }
+    }
+    const float *b(int l) const { return w + off[2 * l + 1]; }
+
+    void gemm(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long M, long N, int K, GemmEpilogue E) {
+        E.err = err;
+        gemmBf16(A, B, M, N, K, E, st);
+    }
+    // [hi | lo] rows of an activation (rows x d) as the A operand of a product with weights
+    void splitRows(const float *src, int rows, int dd, __nv_bfloat16 *dst) {
+        k_split_rows<<<grid1((size_t)rows * pad64(dd)), 256, 0, st>>>(src, rows, dd, dst, pad64(dd), 2, 0b10);
         MCK(cudaGetLastError());
     }
-    const __nv_bfloat16 *W(int l) const { return wb + off[2 * l]; }
-    const float *b(int l) const { return w + off[2 * l + 1]; }
+    // transposed three-segment operands of a weight gradient: A = [hi|lo|hi], B = [hi|hi|lo]
+    void splitCols(const float *src, int rows, int dd, __nv_bfloat16 *dst, int loMask) {
+        dim3 grid((unsigned)((pad64(rows) + 31) / 32), (unsigned)((dd + 31) / 32));
+        k_split_cols<<<grid, 256, 0, st>>>(src, rows, dd, dst, pad64(rows), 3, loMask);
+        MCK(cudaGetLastError());
+    }
+    void checkErr() {
+        int h = 0;
+        MCK(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        MCK(cudaStreamSynchronize(st));
+        if (h) throw std::runtime_error("[mlp] the tensor-core pipeline gave up (code " + std::to_string(h) + ")");
+    }
+
+    // layer l: out (cols x d[l+1]) = in (cols x d[l]) W' + b, and its GELU when act
+    void layer(int l, const float *in, int cols, float *pre, float *act) {
+        splitRows(in, cols, d[l], opA);
+        GemmEpilogue E;
+        E.colAdd = b(l);
+        E.D = pre;
+        E.ldd = d[l + 1];
+        if (act) {
+            E.gelu = 1;
+            E.Dact = act;
+        }
+        gemm(opA, wr[l], cols, d[l + 1], 2 * dP[l], E);
+    }
 
     void forward(const float *X, int cols) {
         reserve(cols);
-        gemm(st, d[1], cols, d[0], 1.f, W(0), d[1], false, X, d[0], false, 0.f, A1, d[1]);
-        k_bias_act<<<grid1((size_t)d[1] * cols), 256, 0, st>>>(A1, H1, b(0), d[1], cols, 1);
-        gemm(st, d[2], cols, d[1], 1.f, W(1), d[2], false, H1, d[1], false, 0.f, A2, d[2]);
-        k_bias_act<<<grid1((size_t)d[2] * cols), 256, 0, st>>>(A2, H2, b(1), d[2], cols, 1);
-        gemm(st, d[3], cols, d[2], 1.f, W(2), d[3], false, H2, d[2], false, 0.f, Y, d[3]);
-        k_bias_act<<<grid1((size_t)d[3] * cols), 256, 0, st>>>(Y, Y, b(2), d[3], cols, 0);
+        layer(0, X, cols, A1, H1);
+        layer(1, H1, cols, A2, H2);
+        layer(2, H2, cols, Y, nullptr);
+    }
+
+    // dW of layer l (column-major d[l+1] x d[l], i.e. row-major d[l] x d[l+1]) = sum over samples of
+    // in[s][i] dA[s][o], into g.
+    void weightGrad(int l, const float *in, const float *dA, int cols) {
+        splitCols(in, cols, d[l], opA, 0b010);
+        splitCols(dA, cols, d[l + 1], opB, 0b100);
+        GemmEpilogue E;
+        E.D = g + off[2 * l];
+        E.ldd = d[l + 1];
+        gemm(opA, opB, d[l], d[l + 1], 3 * pad64(cols), E);
+        k_rowsum<<<(d[l + 1] + 255) / 256, 256, 0, st>>>(dA, g + off[2 * l + 1], d[l + 1], cols);
         MCK(cudaGetLastError());
+    }
+    // dH (cols x d[l]) = dA (cols x d[l+1]) W_l
+    void dataGrad(int l, const float *dA, int cols, float *out) {
+        splitRows(dA, cols, d[l + 1], opA);
+        GemmEpilogue E;
+        E.D = out;
+        E.ldd = d[l];
+        gemm(opA, wc[l], cols, d[l], 2 * dP[l + 1], E);
     }
 
     // Gradients of the mean squared error into g (same packing as w); returns the loss.
     float backward(const float *X, const float *T, int cols) {
         MCK(cudaMemsetAsync(loss, 0, sizeof(float), st));
         k_mse<<<grid1((size_t)d[3] * cols), 256, 0, st>>>(Y, T, dY, d[3], cols, loss);
-        // layer 3: dW3 = dY H2', db3 = rowsum dY, dH2 = W3' dY
-        gemm(st, d[3], d[2], cols, 1.f, dY, d[3], false, H2, d[2], true, 0.f, g + off[4], d[3]);
-        k_rowsum<<<(d[3] + 255) / 256, 256, 0, st>>>(dY, g + off[5], d[3], cols);
-        gemm(st, d[2], cols, d[3], 1.f, W(2), d[3], true, dY, d[3], false, 0.f, dH, d[2]);
-        k_gelu_back<<<grid1((size_t)d[2] * cols), 256, 0, st>>>(dH, A2, (size_t)d[2] * cols);
-        // layer 2: dW2 = dA2 H1', db2, dH1 = W2' dA2 (dA2 is kept in A2's place after use)
-        gemm(st, d[2], d[1], cols, 1.f, dH, d[2], false, H1, d[1], true, 0.f, g + off[2], d[2]);
-        k_rowsum<<<(d[2] + 255) / 256, 256, 0, st>>>(dH, g + off[3], d[2], cols);
-        MCK(cudaMemcpyAsync(A2, dH, sizeof(float) * (size_t)d[2] * cols, cudaMemcpyDeviceToDevice, st));
-        gemm(st, d[1], cols, d[2], 1.f, W(1), d[2], true, A2, d[2], false, 0.f, dH, d[1]);
-        k_gelu_back<<<grid1((size_t)d[1] * cols), 256, 0, st>>>(dH, A1, (size_t)d[1] * cols);
-        // layer 1: dW1 = dA1 X', db1
-        gemm(st, d[1], d[0], cols, 1.f, dH, d[1], false, X, d[0], true, 0.f, g + off[0], d[1]);
-        k_rowsum<<<(d[1] + 255) / 256, 256, 0, st>>>(dH, g + off[1], d[1], cols);
         MCK(cudaGetLastError());
+        weightGrad(2, H2, dY, cols);
+        dataGrad(2, dY, cols, dH);
+        k_gelu_back<<<grid1((size_t)d[2] * cols), 256, 0, st>>>(dH, A2, (size_t)d[2] * cols);  // dA2
+        MCK(cudaGetLastError());
+        weightGrad(1, H1, dH, cols);
+        dataGrad(1, dH, cols, dH);  // the operand copy of dA2 is taken before dH is overwritten
+        k_gelu_back<<<grid1((size_t)d[1] * cols), 256, 0, st>>>(dH, A1, (size_t)d[1] * cols);  // dA1
+        MCK(cudaGetLastError());
+        weightGrad(0, X, dH, cols);
         float l = 0.f;
         MCK(cudaMemcpyAsync(&l, loss, sizeof(float), cudaMemcpyDeviceToHost, st));
-        MCK(cudaStreamSynchronize(st));
+        checkErr();
         return l;
     }
 
@@ -264,8 +319,9 @@ struct Mlp {
         steps++;
         const float b1 = .9f, b2 = .999f;
         const float c1 = 1.f - powf(b1, (float)steps), c2 = 1.f - powf(b2, (float)steps);
-        k_adam<<<grid1(total), 256, 0, st>>>(w, wb, g, mo, v, total, lr, b1, b2, 1e-8f, c1, c2);
+        k_adam<<<grid1(total), 256, 0, st>>>(w, g, mo, v, total, lr, b1, b2, 1e-8f, c1, c2);
         MCK(cudaGetLastError());
+        refreshBf16();
     }
 };
 
@@ -317,7 +373,7 @@ int spock_mlp_forward(spock_mlp h, const void *x_device, int cols, void *y_devic
         spock::Mlp &m = *h->m;
         m.forward((const float *)x_device, cols);
         MCK(cudaMemcpyAsync(y_device, m.Y, sizeof(float) * (size_t)m.d[3] * cols, cudaMemcpyDeviceToDevice, m.st));
-        MCK(cudaStreamSynchronize(m.st));
+        m.checkErr();
     });
 }
 

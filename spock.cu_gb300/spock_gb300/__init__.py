@@ -90,6 +90,10 @@ _SIGS = {
     "spock_resolve": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.c_long, _ip, _lp]),
     "spock_resolve_device": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _ip, _lp]),
     "spock_project_dynamics_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    "spock_get_dual": (ctypes.c_int, [_vp, _dp, _dp]),
+    "spock_gemm_bf16": (ctypes.c_int, [_vp, _vp, ctypes.c_long, ctypes.c_long, ctypes.c_int, ctypes.c_float, _vp, _vp,
+                                       ctypes.c_int, _vp, _vp, ctypes.c_long, ctypes.c_int]),
+    "spock_warm_start_pca": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, _vp]),
 }
 
 _lib = None
@@ -390,6 +394,16 @@ class Cache:
         z = np.ascontiguousarray(z, dtype=np.float64)
         out = np.zeros(self.sizeIterate())
         _check(lib().spock_cp_step(self._h, _p(x0), _p(z), _p(out)))
+        return out
+
+    def getDual(self, primal):
+        """Cache::getDual (cache.cuh:371-376): the dual candidate for the primal candidate
+        `primal` at the current iterate."""
+        primal = np.ascontiguousarray(primal, dtype=np.float64)
+        if primal.shape != (self.sizePrimal(),):
+            raise ValueError("[getDual] primal has the wrong size")
+        out = np.zeros(self.sizeDual())
+        _check(lib().spock_get_dual(self._h, _p(primal), _p(out)))
         return out
 
     def applyM(self, z):

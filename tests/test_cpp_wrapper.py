@@ -56,6 +56,7 @@ def test_cpp_solve_matches_oracle(exe, oracle_lib):
     status, iters = int(lines[0].split()[0]), int(lines[0].split()[1])
     assert status == 0 and iters > 0
     u0 = np.array([float(v) for v in lines[1:1 + P.nu]])
+    assert lines[1 + P.nu].startswith("getDual") and float(lines[1 + P.nu].split()[1]) < 1e-6
     z, s = P.run(x0, oracle_lib.options(tol=1e-10, max_iters=20000), "spock")
     u_ref = P.states_inputs(z)[1][:P.nu]
     assert np.abs(u0 - u_ref).max() <= 1e-8 * max(1., np.abs(u_ref).max())

@@ -443,3 +443,17 @@ def test_polyhedron_with_identity(oracle_lib, tmp_path, batch):
     assert s.status == 0
     u_ref = P.states_inputs(z)[1][:P.nu]
     assert np.abs(c.inputs()[:P.nu] - u_ref).max() <= 1e-5 * max(1., np.abs(u_ref).max())
+
+
+@pytest.mark.parametrize("precision,tol,batch", [(64, 1e-10, 1), (32, 1e-4, 32)])
+def test_get_dual(oracle_lib, precision, tol, batch):
+    """Cache::getDual (cache.cuh:371-376): at the iterate z, the dual candidate for the primal
+    half of T(z) is the dual half of T(z) (the oracle's CP step)."""
+    path = os.path.join(GOLDEN, "cfg1")
+    t, d, c = make(path, precision, batch=batch)
+    P = oracle_lib.Problem(path)
+    x0 = golden("cfg1", "initialState_d.bt")
+    z = np.random.default_rng(12).standard_normal(P.size)
+    c.cpStep(x0, z)  # leaves z as the solver's iterate
+    ref = P.cp_step(x0 * P.scaling[:P.nx], z)
+    assert rel(c.getDual(ref[:P.size_prim]), ref[P.size_prim:]) < tol
