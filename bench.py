@@ -49,6 +49,20 @@ def parse():
     ap.add_argument("--max-iters", type=int, default=20000)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-fp64-baseline", action="store_true", help="skip the plain FP64 SPOCK solves on the GPU")
+    ap.add_argument("--study", choices=["warmstart", "precision", "mixed"],
+                    help="instead of the benchmark line: the learned warm start (config 5), the precision study "
+                         "(config 3) or the mixed batch (config 4 mixed); one JSON line per result")
+    ap.add_argument("--train", type=int, default=16384, help="warmstart: training solves")
+    ap.add_argument("--pca-rows", type=int, default=8192, help="warmstart: solutions the PCA basis is fitted on")
+    ap.add_argument("--train-tol", type=float, default=1e-4, help="warmstart: tolerance of the training solves")
+    ap.add_argument("--test", type=int, default=10240, help="warmstart: held-out initial states")
+    ap.add_argument("--epochs", type=int, default=40, help="warmstart: MLP training epochs")
+    ap.add_argument("--kernels", help="instead of the benchmark line: comma-separated round kernels (lstar, lop, "
+                                      "mlstar, mlop, dyn, reduce, update, round) timed one launch at a time on a "
+                                      "random iterate of --batch instances, tiles 1 per CTA (profiling driver)")
+    ap.add_argument("--kernel-reps", type=int, default=5, help="kernels: timed launches after one untimed")
+    ap.add_argument("--gemm", action="store_true", help="instead of the benchmark line: the tensor-core GEMM at the "
+                                                        "warm start's reconstruction shape and an MLP shape")
     return ap.parse_args()
 
 
@@ -387,8 +401,276 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def study_warmstart(args):
+    """Learned warm start on the benchmark's problem family (config 5 at a stated scale): train
+    data = cold FP32 batch solves of x0 ~ U[-1, 1]^50 at tol(--train-tol); PCA(128) of the first
+    --pca-rows solutions; MLP 50 -> 1024 -> 1024 -> 128 (the library's tensor-core kernels) on
+    the coefficients of all of them; then --test held-out x0 in batches of 1,024 solved to the
+    absolute tolerance 1e-4 (a warm start's initial error is small, so tol(1e-4) decides by its
+    absolute part; the cold comparison is held to the same absolute tolerance) from: a cold
+    start, the learned start, and the previous held-out instance's solution (the shifted
+    previous solution of a stream of requests).  Prints one JSON line per phase and method."""
+    import torch
+    import spock_gb300 as sg
+    from spock_gb300.warmstart import PcaMlpWarmStart
+    sg.build()
+    B = 1024
+    path, _ = workload(args.seed, 1)
+    t = sg.ScenarioTree(path)
+    d = sg.ProblemData(t)
+    rng = np.random.default_rng(2026 + args.seed)
+    ntr = (args.train + B - 1) // B * B
+    nte = max(B, args.test // B * B)
+    xtr = rng.uniform(-1., 1., (ntr, t.numStates()))
+    xte = rng.uniform(-1., 1., (nte, t.numStates()))
+
+    def cache(absolute, tol=1e-4):
+        b = sg.CacheBuilder(t, d).andersonBuffer(ANDERSON).maxIters(args.max_iters).precision(32).batch(B)
+        b = b.toleranceAbsolute(tol).toleranceRelative(0.) if absolute else b.tol(tol)
+        return b.build()
+
+    def emit(rec):
+        print(json.dumps(rec), flush=True)
+
+    ws = PcaMlpWarmStart(k=128, hidden=1024, seed=args.seed)
+    ctr = cache(False, args.train_tol)
+    t0 = time.time()
+    zs, coefs, conv = [], [], 0
+    for s0 in range(0, ntr, B):
+        conv += int((ctr.runSpockBatch(xtr[s0:s0 + B]) == 0).sum())
+        z = torch.tensor(ctr.solutions(), dtype=torch.float32, device="cuda")
+        if s0 < args.pca_rows:
+            zs.append(z)
+            if s0 + B >= min(args.pca_rows, ntr):
+                ws.fit_basis(torch.cat(zs))
+                coefs += [ws.project(zz) for zz in zs]
+                zs = []
+        else:
+            coefs.append(ws.project(z))
+    emit({"study": "warmstart", "phase": "data", "solves": ntr, "converged": conv, "tol": args.train_tol,
+          "seconds": round(time.time() - t0, 1), "pca_rows": min(args.pca_rows, ntr), "pca_explained": ws.explained})
+    t0 = time.time()
+    losses = ws.fit_mlp(xtr, torch.cat(coefs), epochs=args.epochs, batch=B, lr=1e-3)
+    emit({"study": "warmstart", "phase": "fit", "seconds": round(time.time() - t0, 1), "epochs": args.epochs,
+          "loss_first": losses[0], "loss_last": losses[-1]})
+    methods = ("cold_tol", "cold_absolute", "learned", "shifted_previous")
+    res = {m: {"seconds": 0., "iters": [], "conv": 0, "u0_err": 0., "n": 0} for m in methods}
+    cc, ca, cw, cp = cache(False), cache(True), cache(True), cache(True)
+    z_prev = None  # the last solution of the previous batch (instance B-1)
+
+    def timed(name, c, f, x):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        st = f()
+        res[name]["seconds"] += time.perf_counter() - t1
+        res[name]["iters"].append(c.solveIters())
+        res[name]["conv"] += int((st == 0).sum())
+        res[name]["n"] += len(x)
+        return st
+
+    for s0 in range(0, nte, B):
+        x = xte[s0:s0 + B]
+        # cold, reference tolerance semantics: tol(1e-4) captures its relative part (~1e-3 here)
+        timed("cold_tol", cc, lambda: cc.runSpockBatch(x), x)
+        u_cold = cc.firstInputs()
+        z_cold = torch.tensor(cc.solutions(), dtype=torch.float32, device="cuda")
+        if s0 == 0:  # cold at the warm starts' absolute tolerance: the equal-accuracy comparison (one batch)
+            timed("cold_absolute", ca, lambda: ca.runSpockBatch(x), x)
+        # previous request's solution: instance i starts from instance i-1's (the first from the
+        # previous batch's last)
+        prev = torch.roll(z_cold, 1, 0)
+        if z_prev is not None:
+            prev[0] = z_prev
+        z_prev = z_cold[-1].clone()
+        zp = prev.T.contiguous()
+        cp.setIterateDevice(zp.data_ptr(), 32)
+        timed("shifted_previous", cp, lambda: cp.resolveBatch(x), x)
+        timed("learned", cw, lambda: (ws.warm_start(cw, x), cw.resolveBatch(x))[1], x)  # prediction included
+        for name, c in (("shifted_previous", cp), ("learned", cw)):
+            res[name]["u0_err"] = max(res[name]["u0_err"], float(np.abs(c.firstInputs() - u_cold).max()))
+    for name, r in res.items():
+        it = np.concatenate(r["iters"])
+        emit({"study": "warmstart", "method": name, "instances": r["n"], "batch": B, "converged": r["conv"],
+              "solves_per_s": r["n"] / r["seconds"], "iters_mean": float(it.mean()), "iters_max": int(it.max()),
+              "u0_max_diff_vs_cold_tol": r["u0_err"] if name in ("learned", "shifted_previous") else None,
+              "tolerance": "tol(1e-4), relative part decides" if name == "cold_tol" else "absolute 1e-4 (relative 0)"})
+
+
+def study_precision(args):
+    """Config 3 (i.i.d. 5 events, N=8, stopping 3: 781 nodes; nx=100, nu=40; box on x; AVaR 0.9)
+    with costs x 1e-3 (at the literal scale SPOCK stalls on this problem in FP64 too, as on
+    config 2), with the input ball ||u||_2 <= 2 and with the input box |u_i| <= 2.  Eight
+    initial states (32 GPU instances, rows reused) solved cold:
+      * FP32 on the GPU (batched kernels) to tol(1e-4) and to tol(1e-6);
+      * the FP64 oracle on the host cores to tol(1e-4) (at most 1,500 iterations, 240 s);
+      * (input box) the FP64 polish on the GPU of the FP32 solution to tol(1e-6), the tight
+        reference (FP64 with the input ball exceeds the kernels' shared memory at this size).
+    Errors of each FP32 result against the FP64 ones: relative error of the optimal cost s_0 and
+    max error of the unscaled states and inputs.  One JSON line per comparison."""
+    import spock_gb300 as sg
+    from oracle import oracle
+    from spock_gb300 import configs
+    sg.build()
+    oracle.build()
+    n, B = 8, 32
+    for ball in (True, False):
+        path, x0 = configs.cached("config3", PROBLEM_DIR, seed=args.seed, count=n, ball=ball, cost_scale=COST_SCALE)
+        xb = np.resize(x0, (B, x0.shape[1]))
+        t = sg.ScenarioTree(path)
+        d = sg.ProblemData(t)
+        P = oracle.Problem(path)
+        oS = P.size_prim - P.n
+        name = "config3 x 1e-3 " + ("input ball" if ball else "input box")
+        t0 = time.time()
+        zr = np.zeros((n, P.size))
+        _, st_r, it_r, _, _ = P.solve_many_warm(x0, zr, oracle.options(tol=1e-4, anderson=ANDERSON, max_iters=1500,
+                                                                       max_time=240.), n, warm=False)
+        ref = {"oracle fp64 tol(1e-4)": (zr, np.array([P.states_inputs(z)[0] for z in zr]),
+                                         np.array([P.states_inputs(z)[1] for z in zr]),
+                                         f"{int((st_r == 0).sum())}/{n} converged, {np.mean(it_r):.0f} iterations, "
+                                         f"{time.time() - t0:.0f} s on {n} threads")}
+
+        def gpu(c):
+            return (np.stack([c.solution(b) for b in range(n)]), np.stack([c.states(b) for b in range(n)]),
+                    np.stack([c.inputs(b) for b in range(n)]))
+        res = {}
+        for eps in (1e-4, 1e-6):
+            c = (sg.CacheBuilder(t, d).tol(eps).andersonBuffer(ANDERSON).maxIters(args.max_iters).precision(32)
+                 .batch(B).build())
+            t1 = time.time()
+            c.runSpockBatch(xb)
+            res[eps] = (c, time.time() - t1)
+            if eps == 1e-6 and not ball:
+                c64 = (sg.CacheBuilder(t, d).tol(eps).andersonBuffer(ANDERSON).maxIters(args.max_iters)
+                       .precision(64).batch(B).build())
+                t1 = time.time()
+                st64 = c64.polish(c, xb)
+                ref["gpu fp32 + fp64 polish tol(1e-6)"] = gpu(c64) + (
+                    f"{int((st64[:n] == 0).sum())}/{n} converged, {np.mean(c64.solveIters()[:n]):.0f} iterations, "
+                    f"{time.time() - t1:.1f} s",)
+        for eps, (c, secs) in res.items():
+            zg, xg, ug = gpu(c)
+            for rname, (zr_, xr_, ur_, note) in ref.items():
+                print(json.dumps({"study": "precision", "problem": name, "solver": f"gpu fp32 tol({eps:g})",
+                                  "converged": int((c.statuses()[:n] == 0).sum()), "instances": n,
+                                  "iters_mean": float(np.mean(c.solveIters()[:n])), "seconds": round(secs, 2),
+                                  "against": rname, "against_run": note,
+                                  "cost_rel_err_max": float(np.max(np.abs(zg[:, oS] - zr_[:, oS]) / np.abs(zr_[:, oS]))),
+                                  "states_err_max": float(np.abs(xg - xr_).max()),
+                                  "inputs_err_max": float(np.abs(ug - ur_).max()),
+                                  "u0_err_max": float(np.abs(ug[:, :P.nu] - ur_[:, :P.nu]).max())}), flush=True)
+
+
+def kernel_times(args):
+    """Profiling driver: an FP32 solver of --batch instances of the benchmark's problem with a
+    random iterate (N(0, 0.25) entries), instance tiles 1 per CTA, and single launches of the
+    named round kernels (one untimed, then --kernel-reps timed with CUDA events on the solver's
+    stream).  Prints kernel, ms per launch and algorithmic GB/s."""
+    import torch
+    import spock_gb300 as sg
+    sg.build()
+    B = args.batch
+    path, _ = workload(args.seed, 1)
+    t = sg.ScenarioTree(path)
+    d = sg.ProblemData(t)
+    c = sg.CacheBuilder(t, d).tol(TOL).andersonBuffer(ANDERSON).precision(32).batch(B).build()
+    c.setTuning(1, 1, 1)
+    g = torch.Generator(device="cuda").manual_seed(args.seed)
+    z = (0.5 * torch.randn(c.sizeIterate(), B, device="cuda", generator=g)).contiguous()
+    c.setIterateDevice(z.data_ptr(), 32)
+    torch.cuda.synchronize()
+    for k in args.kernels.split(","):
+        ms, by = c.kernelTime(k, args.kernel_reps)
+        print(json.dumps({"kernel": k, "batch": B, "ms": ms, "algorithmic_bytes": by,
+                          "gbs": by / ms / 1e6 if by else None}), flush=True)
+
+
+def gemm_times(args):
+    """Profiling driver: spock_gemm_bf16 at the warm start's reconstruction shape (M = 138,760
+    iterate entries, N = 1,024 instances, K = 384: BF16 hi/lo segments of 128 basis columns) and
+    at an MLP shape (1,024 x 1,024, K = 2,048), three launches each, CUDA events."""
+    import ctypes
+    import torch
+    import spock_gb300 as sg
+    sg.build()
+    vp = ctypes.c_void_p
+    for (M, N, K) in [(138760, 1024, 384), (1024, 1024, 2048)]:
+        A = torch.randn(M, K, device="cuda").to(torch.bfloat16)
+        Bm = torch.randn(N, K, device="cuda").to(torch.bfloat16)
+        D = torch.empty(M, N, device="cuda")
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            rc = sg.lib().spock_gemm_bf16(vp(A.data_ptr()), vp(Bm.data_ptr()), M, N, K, 1.0, None, None, 0,
+                                          vp(D.data_ptr()), None, N, 0)
+            e1.record()
+            torch.cuda.synchronize()
+            if rc:
+                raise RuntimeError(sg.lib().spock_last_error().decode())
+            ms = e0.elapsed_time(e1)
+            print(json.dumps({"M": M, "N": N, "K": K, "ms": ms, "tflops": 2 * M * N * K / ms / 1e9,
+                              "gbs_moved": (M * K * 2 + N * K * 2 + M * N * 4) / ms / 1e6}), flush=True)
+
+
+def study_mixed(args):
+    """Config 4's mixed batch: 256 problems, each from its own seed, nx ~ U{8..96}, nu = nx/2,
+    Markov chains of 2-4 states, horizons 5-15, stopping stage 2-4, costs x 1e-3, one initial
+    state each, FP32 SPOCK to tol(1e-4) with Anderson memory 5.  Timed: the group solve (every
+    round one CUDA graph over all running solvers, spock_solve_group) and the same solves one
+    after another.  Problems are written by a process pool before the GPU is touched."""
+    from spock_gb300 import configs
+    t0 = time.perf_counter()
+    problems = configs.config4_mixed(PROBLEM_DIR, seed=args.seed, count=256, workers=os.cpu_count() or 1)
+    print(json.dumps({"study": "mixed", "phase": "problems written", "seconds": round(time.perf_counter() - t0, 1)}),
+          flush=True)
+    import spock_gb300 as sg
+    sg.build()
+    caches, x0s, dims = [], [], []
+    for path, x0 in problems:
+        t = sg.ScenarioTree(path)
+        d = sg.ProblemData(t)
+        caches.append(sg.CacheBuilder(t, d).tol(TOL).andersonBuffer(ANDERSON).maxIters(args.max_iters).precision(32)
+                      .batch(1).build())
+        x0s.append(x0[None, :])
+        dims.append((t.numStates(), t.numNodes()))
+    sg.solve_group(caches, x0s)  # warm-up: each solver captures its round graph
+    t0 = time.perf_counter()
+    sts = sg.solve_group(caches, x0s)
+    t_group = time.perf_counter() - t0
+    it_group = np.array([c.solveIter() for c in caches])
+    nx = np.array([q[0] for q in dims])
+    nodes = np.array([q[1] for q in dims])
+    base = {"study": "mixed", "problems": len(caches), "precision": "fp32", "tol": TOL,
+            "nx_range": [int(nx.min()), int(nx.max())], "nodes_range": [int(nodes.min()), int(nodes.max())]}
+    print(json.dumps(dict(base, method="group (one CUDA graph per round)", solves_per_s=len(caches) / t_group,
+                          seconds=t_group, converged=int(sum(int(s[0] == 0) for s in sts)),
+                          iters_mean=float(it_group.mean()), iters_max=int(it_group.max()))), flush=True)
+    t0 = time.perf_counter()
+    st_seq = [c.runSpock(x[0]) for c, x in zip(caches, x0s)]
+    t_seq = time.perf_counter() - t0
+    it_seq = np.array([c.solveIter() for c in caches])
+    print(json.dumps(dict(base, method="one after another", solves_per_s=len(caches) / t_seq, seconds=t_seq,
+                          converged=int(sum(s == 0 for s in st_seq)), iters_mean=float(it_seq.mean()),
+                          iters_max=int(it_seq.max()), same_iterations=bool((it_seq == it_group).all()))), flush=True)
+
+
 def main():
     args = parse()
+    if args.kernels:
+        kernel_times(args)
+        return
+    if args.gemm:
+        gemm_times(args)
+        return
+    if args.study == "mixed":
+        study_mixed(args)
+        return
+    if args.study == "warmstart":
+        study_warmstart(args)
+        return
+    if args.study == "precision":
+        study_precision(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -90,8 +90,10 @@ int spock_solve(spock_solver s, int algo, const double *x0, long count, const do
 int spock_solve_device(spock_solver s, int algo, const void *x0_device, int *statuses, long *iters);
 
 /* Mixed batches (instances of different trees and dimensions, one solver per problem): cold-start
- * solves of `count` distinct solvers at once, one host thread each, every solver on its own CUDA
- * stream so the GPU runs them concurrently; returns when all have stopped.  x0s[i] holds
+ * solves of `count` distinct solvers at once; returns when all have stopped.  SPOCK solves on one
+ * device run as one launch sequence: each round is a single CUDA graph holding every running
+ * solver's round, so the GPU runs the solvers' kernels side by side (finished solvers leave the
+ * graph); CP solves, or solvers on several devices, run one host thread each.  x0s[i] holds
  * x0counts[i] rows for solver i (as spock_solve); statuses[i] / iters[i] (batch entries each) may be
  * NULL, as may statuses / iters.  No reference counterpart. */
 int spock_solve_group(long count, spock_solver *solvers, int algo, const double *const *x0s, const long *x0counts,
@@ -142,6 +144,11 @@ int spock_apply_m(spock_solver s, const double *z, double *mz);            /* M 
  * for a given primal candidate `prim` (sizePrimal values) at the solver's current iterate z
  * (instance 0; for a batch, every instance gets `prim`); `dual` receives sizeDual values. */
 int spock_get_dual(spock_solver s, const double *prim, double *dual);
+/* The reductions a SuperMann round makes on the device, for a residual r and M r (sizeIterate
+ * values each, instance 0): out3 = {r'Mr (the square of normM, cache.cuh:721-742), max|Mr| (the
+ * error check's maximum, cache.cuh:909-961), r'r}, as the controller receives them (FP64 sums of
+ * the kernels' partials).  A check of their accuracy for FP32 solvers; no reference counterpart. */
+int spock_reduce_check(spock_solver s, const double *r, const double *mr, double *out3);
 
 /* Measurement hooks for the benchmark: CUDA-event time of one launch of a named kernel
  * ("lstar", "lop", "mlstar", "mlop", "dyn", "reduce", "update", "teval", "round"), its
@@ -190,7 +197,7 @@ int spock_project_dynamics_noalloc(spock_solver s, const void *x0, void *prim_ux
  * (M x K) and B (N x K) BF16 device arrays, row-major with K contiguous, K a multiple of 64,
  * FP32 accumulation; D (FP32 row-major M x N, leading dimension ldd) gets the sum and Dact its
  * GELU (tanh form) when gelu is nonzero; either may be NULL.  Synchronous on `device`.
- * spock_warm_start_pca: sets an FP32 solver's iterate to mean + basis coef' (basis: sizeIterate x
+ * spock_warm_start_pca: sets a solver's iterate to mean + basis coef' (basis: sizeIterate x
  * k, coef: batch x k, BF16 row-major, k a multiple of 64; mean: sizeIterate FP32 values, all
  * device arrays) with the same GEMM writing the solver's element-major iterate directly; then
  * re-solve with spock_resolve. */

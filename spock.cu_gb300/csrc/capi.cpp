@@ -197,6 +197,112 @@ int spock_offline_dynamics(spock_problem pp, int device, int replace, double *P,
     });
 }
 
+// Active instances of each solver of a group: out[e] = number of statuses -1 of solver e.
+__global__ void k_group_active(const int *const *status, const long *batch, int count, int *out) {
+    const int e = blockIdx.x;
+    if (e >= count) return;
+    int c = 0;
+    for (long b = threadIdx.x; b < batch[e]; b += blockDim.x) c += status[e][b] == -1;
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    __shared__ int part[32];
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int s = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += part[w];
+        out[e] = s;
+    }
+}
+
+#define GCK(x)                                                                                     \
+    do {                                                                                           \
+        cudaError_t e_ = (x);                                                                      \
+        if (e_ != cudaSuccess) throw std::runtime_error(std::string("[solveGroup] ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+// SPOCK solves of several solvers (different problems, one device) as one launch sequence: every
+// round is a single CUDA graph holding each still-running solver's captured round as a child
+// graph, so the solvers' node kernels run side by side; every 10 rounds one kernel counts each
+// solver's running instances, and the graph is rebuilt without the finished solvers whenever a
+// quarter of the remaining ones (at least one) has finished.
+static void solveGroupGraph(const std::vector<spock_solver_s *> &sv, int device) {
+    const int n = (int)sv.size();
+    GCK(cudaSetDevice(device));
+    for (auto *s : sv) s->eng->groupBegin(false);
+    cudaStream_t st = nullptr;
+    const int **dStatus = nullptr;
+    long *dBatch = nullptr;
+    int *dActive = nullptr, *hActive = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    auto cleanup = [&] {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (st) cudaStreamSynchronize(st);
+        cudaFree(dStatus);
+        cudaFree(dBatch);
+        cudaFree(dActive);
+        if (hActive) cudaFreeHost(hActive);
+        if (st) cudaStreamDestroy(st);
+    };
+    try {
+        GCK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        std::vector<const int *> hs((size_t)n);
+        std::vector<long> hb((size_t)n);
+        for (int e = 0; e < n; e++) {
+            hs[(size_t)e] = sv[(size_t)e]->eng->statusDevice();
+            hb[(size_t)e] = sv[(size_t)e]->eng->batch();
+        }
+        GCK(cudaMalloc(&dStatus, sizeof(int *) * n));
+        GCK(cudaMalloc(&dBatch, sizeof(long) * n));
+        GCK(cudaMalloc(&dActive, sizeof(int) * n));
+        GCK(cudaMallocHost(&hActive, sizeof(int) * n));
+        GCK(cudaMemcpy(dStatus, hs.data(), sizeof(int *) * n, cudaMemcpyHostToDevice));
+        GCK(cudaMemcpy(dBatch, hb.data(), sizeof(long) * n, cudaMemcpyHostToDevice));
+        std::vector<char> alive((size_t)n, 1);
+        std::vector<long> rounds((size_t)n, 0);
+        int nAlive = n, aliveAtBuild = 0;
+        auto build = [&] {
+            if (exec) GCK(cudaGraphExecDestroy(exec));
+            exec = nullptr;
+            cudaGraph_t g;
+            GCK(cudaGraphCreate(&g, 0));
+            for (int e = 0; e < n; e++)
+                if (alive[(size_t)e]) {
+                    cudaGraphNode_t node;
+                    GCK(cudaGraphAddChildGraphNode(&node, g, nullptr, 0, sv[(size_t)e]->eng->roundGraph()));
+                }
+            const cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
+            cudaGraphDestroy(g);
+            GCK(ie);
+            aliveAtBuild = nAlive;
+        };
+        build();
+        long r = 0;
+        while (nAlive > 0) {
+            GCK(cudaGraphLaunch(exec, st));
+            r++;
+            for (int e = 0; e < n; e++)
+                if (alive[(size_t)e]) rounds[(size_t)e] = r;
+            if (r % 10) continue;
+            k_group_active<<<n, 128, 0, st>>>(dStatus, dBatch, n, dActive);
+            GCK(cudaGetLastError());
+            GCK(cudaMemcpyAsync(hActive, dActive, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+            GCK(cudaStreamSynchronize(st));
+            for (int e = 0; e < n; e++)
+                if (alive[(size_t)e] && hActive[e] == 0) {
+                    alive[(size_t)e] = 0;
+                    nAlive--;
+                }
+            if (nAlive > 0 && aliveAtBuild - nAlive >= std::max(1, aliveAtBuild / 4)) build();
+        }
+        GCK(cudaStreamSynchronize(st));
+        for (int e = 0; e < n; e++) sv[(size_t)e]->eng->groupEnd(rounds[(size_t)e]);
+    } catch (...) {
+        cleanup();
+        throw;
+    }
+    cleanup();
+}
+
 int spock_solve_group(long count, spock_solver *solvers, int algo, const double *const *x0s, const long *x0counts,
                       int *const *statuses, long *const *iters) {
     return guard([&] {
@@ -207,6 +313,20 @@ int spock_solve_group(long count, spock_solver *solvers, int algo, const double 
             need(x0s[i], "x0");
             for (long j = 0; j < i; j++)
                 if (solvers[j] == solvers[i]) throw std::invalid_argument("[solveGroup] a solver appears twice");
+        }
+        bool oneDevice = true;
+        for (long i = 1; i < count; i++) oneDevice = oneDevice && solver(solvers[i])->eng->device() == solver(solvers[0])->eng->device();
+        if (algo == SPOCK_ALGO_SPOCK && oneDevice) {
+            std::vector<spock_solver_s *> sv;
+            for (long i = 0; i < count; i++) {
+                auto *s = solver(solvers[i]);
+                GCK(cudaSetDevice(s->eng->device()));
+                s->eng->setInitialStates(x0s[i], x0counts[i]);
+                sv.push_back(s);
+            }
+            solveGroupGraph(sv, sv[0]->eng->device());
+            for (long i = 0; i < count; i++) finishSolve(sv[(size_t)i], statuses ? statuses[i] : nullptr, iters ? iters[i] : nullptr);
+            return;
         }
         std::vector<std::string> errors((size_t)count);
         std::vector<std::thread> threads;
@@ -370,6 +490,16 @@ int spock_cp_step(spock_solver sv, const double *x0, const double *z, double *ca
         need(z, "z");
         need(cand, "cand");
         s->eng->cpStep(x0, z, cand);
+    });
+}
+
+int spock_reduce_check(spock_solver sv, const double *r, const double *mr, double *out3) {
+    return guard([&] {
+        auto *s = solver(sv);
+        need(r, "r");
+        need(mr, "mr");
+        need(out3, "out3");
+        s->eng->reduceCheck(r, mr, out3);
     });
 }
 

@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -613,6 +614,8 @@ public:
 
     ~Engine() override {
         if (graph_) cudaGraphExecDestroy(graph_);
+        for (auto &kv : graphsLive_) cudaGraphExecDestroy(kv.second);
+        if (graphTemplate_) cudaGraphDestroy(graphTemplate_);
         for (void *p : allocs_) cudaFree(p);
         if (hostActive_) cudaFreeHost(hostActive_);
         if (stream_) cudaStreamDestroy(stream_);
@@ -666,8 +669,8 @@ public:
         fill(Z_, (size_t)D_.sZ * B_, T(0));
     }
 
-    int run(Algo algo, bool warm) override {
-        const auto t0 = std::chrono::steady_clock::now();
+    // The start of a solve: cold or warm buffers (cache.cuh:611-632), controller state, every tile live.
+    void beginSolve(Algo algo, bool warm) {
         const size_t nz = (size_t)D_.sZ * B_;
         if (!warm) fill(Z_, nz, T(0));
         if (algo == kSpock) {
@@ -686,20 +689,43 @@ public:
         allLive();
         capacity_ = B_;
         compactions_ = 0;
+    }
+
+    void groupBegin(bool warm) override {
+        beginSolve(kSpock, warm);
+        ensureGraph();
+        CK(cudaStreamSynchronize(stream_));
+        groupT0_ = std::chrono::steady_clock::now();
+    }
+    cudaGraph_t roundGraph() override {
+        ensureGraph();
+        return graphTemplate_;
+    }
+    const int *statusDevice() const override { return S_.status; }
+    void groupEnd(long rounds) override {
+        lastRounds_ = rounds;
+        lastCompactions_ = 0;
+        lastLaunches_ = (long)launchesPerRound() * rounds + 7;
+        lastSeconds_ = std::chrono::duration<double>(std::chrono::steady_clock::now() - groupT0_).count();
+    }
+
+    int run(Algo algo, bool warm) override {
+        const auto t0 = std::chrono::steady_clock::now();
+        beginSolve(algo, warm);
         int rounds = 0, polls = 0;
         long launches = (algo == kSpock ? 5 : 2) + 2;  // buffer fills + state init + tile flags
         const int poll = B_ > 1 ? 10 : 25;
         if (algo == kSpock) {
-            ensureGraph();
+            cudaGraphExec_t round = graphFor(B_);
             for (;;) {
-                CK(cudaGraphLaunch(graph_, stream_));
+                CK(cudaGraphLaunch(round, stream_));
                 rounds++;
                 launches += launchesPerRound();
                 if (rounds % poll == 0) {
                     polls++;
                     const int act = activeCount(t0);
                     if (act == 0) break;
-                    maybeCompact(act);
+                    if (maybeCompact(act)) round = graphFor(levelFor(capacity_));
                 }
             }
             restoreOrder();
@@ -819,13 +845,14 @@ public:
     }
 
     void warmStartPca(const void *basis, const void *coef, int k, const float *mean) override {
-        if (sizeof(T) != 4) throw std::invalid_argument("[warmStart] the PCA warm start writes FP32 solvers");
         if (!basis || !coef || !mean) throw std::invalid_argument("[warmStart] null device pointer");
         if (!gemmErr_) gemmErr_ = dalloc<int>(1);
         CK(cudaMemsetAsync(gemmErr_, 0, sizeof(int), stream_));
         GemmEpilogue E;
         E.rowAdd = mean;
-        E.D = reinterpret_cast<float *>(Z_);  // element-major sZ x B = row-major with ldd = B
+        // element-major sZ x B = row-major with ldd = B, in the solver's precision
+        if (sizeof(T) == 4) E.D = reinterpret_cast<float *>(Z_);
+        else E.D64 = reinterpret_cast<double *>(Z_);
         E.ldd = B_;
         E.err = gemmErr_;
         gemmBf16(basis, coef, D_.sZ, B_, k, E, stream_);
@@ -833,6 +860,28 @@ public:
         CK(cudaMemcpyAsync(&err, gemmErr_, sizeof(int), cudaMemcpyDeviceToHost, stream_));
         CK(cudaStreamSynchronize(stream_));
         if (err) throw std::runtime_error("[warmStart] the tensor-core pipeline gave up (code " + std::to_string(err) + ")");
+    }
+
+    void reduceCheck(const double *r, const double *mr, double *out3) override {
+        allLive();
+        uploadSlice(R_, r, 0, D_.sZ);
+        uploadSlice(MR_, mr, 0, D_.sZ);
+        const size_t nz = (size_t)D_.sZ * B_;
+        fill(RPREV_, nz, T(0));
+        fill(ANDR_, nz * opt_.anderson, T(0));
+        k_force_phaseA<<<((int)B_ + 127) / 128, 128, 0, stream_>>>(S_, (int)B_, (int)opt_.anderson);
+        CK(cudaGetLastError());
+        reduceLaunch(kSpock, true);
+        std::vector<double> h((size_t)chunks_ * nv_);
+        CK(cudaMemcpyAsync(h.data(), part_, h.size() * sizeof(double), cudaMemcpyDeviceToHost, stream_));  // instance 0
+        CK(cudaStreamSynchronize(stream_));
+        double s0 = 0, mx = 0, s3 = 0;
+        for (int c = 0; c < chunks_; c++) {
+            s0 += h[(size_t)0 * chunks_ + c];
+            mx = std::max(mx, h[(size_t)1 * chunks_ + c]);
+            s3 += h[(size_t)3 * chunks_ + c];
+        }
+        out3[0] = s0; out3[1] = mx; out3[2] = s3;  // c = r - r_prev = r: c'c = r'r
     }
 
     void applyM(const double *z, double *mz) override {
@@ -891,10 +940,7 @@ public:
         tpcDyn_ = dyn;
         backDbl_ = dyn > 1 && canDblBack();
         fwdDbl_ = dyn > 1 && canDblFwd();
-        if (graph_) {  // the captured round has the old launch shapes
-            CK(cudaGraphExecDestroy(graph_));
-            graph_ = nullptr;
-        }
+        dropGraphs();  // the captured rounds have the old launch shapes
     }
 
     void tuning(int *out5) override {
@@ -1018,6 +1064,10 @@ private:
     DevState S_{};
     cudaStream_t stream_ = nullptr;
     cudaGraphExec_t graph_ = nullptr;
+    cudaGraph_t graphTemplate_ = nullptr;
+    std::map<long, cudaGraphExec_t> graphsLive_;  // rounds over fewer slots (after compactions)
+    long gridB_ = 0;                               // slots the launches cover while capturing (0: all)
+    std::chrono::steady_clock::time_point groupT0_;
     std::vector<void *> allocs_;
     T *Z_ = nullptr, *CAND_ = nullptr, *R_ = nullptr, *MR_ = nullptr, *PREV_ = nullptr, *RPREV_ = nullptr;
     T *BACKUP_ = nullptr, *DIR_ = nullptr, *ANDR_ = nullptr, *ANDZ_ = nullptr, *Q_ = nullptr, *DD_ = nullptr;
@@ -1421,7 +1471,7 @@ private:
 
     // L and L*: every node x groups of `tpc` instance tiles; the dynamics sweep: every node of a stage.
     dim3 opGridNodes(int tpc, int nodes) const {
-        const long tiles = (B_ + kTileB - 1) / kTileB;
+        const long tiles = (gB() + kTileB - 1) / kTileB;
         return dim3((unsigned)((tiles + tpc - 1) / tpc), (unsigned)nodes);
     }
     dim3 opGrid(int tpc) const { return opGridNodes(tpc, D_.n); }
@@ -1566,7 +1616,7 @@ private:
         const int TB = B_ >= 32 ? 32 : (int)B_;
         const int lanes = kRedThreads / TB;
         const size_t sm = (size_t)nv_ * lanes * TB * sizeof(double);
-        dim3 grid((unsigned)((B_ + TB - 1) / TB), (unsigned)chunks_);
+        dim3 grid((unsigned)((gB() + TB - 1) / TB), (unsigned)chunks_);
         withAnderson([&](auto mc) { k_reduce<T, decltype(mc)::value><<<grid, kRedThreads, sm, stream_>>>(D_, A); });
         CK(cudaGetLastError());
     }
@@ -1581,7 +1631,7 @@ private:
         A.maxOuter = opt_.maxOuter;
         A.maxInner = opt_.maxInner;
         A.ridge = sizeof(T) == 8 ? 1e-13 : 1e-7;
-        k_control<<<((int)B_ + 3) / 4, 128, 0, stream_>>>((int)B_, A);  // 4 instances (warps) per block
+        k_control<<<((int)gB() + 3) / 4, 128, 0, stream_>>>((int)B_, A);  // 4 instances (warps) per block
         CK(cudaGetLastError());
     }
 
@@ -1597,7 +1647,7 @@ private:
             CK(cudaGetLastError());
             return;
         }
-        const long bx = (B_ + 255) / 256;  // about 8 blocks of 256 threads per SM
+        const long bx = (gB() + 255) / 256;  // about 8 blocks of 256 threads per SM
         const long by = std::max<long>(1, std::min<long>((152 * 8 + bx - 1) / bx, D_.sZ));
         withAnderson([&](auto mc) {
             k_update<T, decltype(mc)::value><<<dim3((unsigned)bx, (unsigned)by), 256, 0, stream_>>>(D_, A);
@@ -1634,12 +1684,14 @@ private:
     // fill at most 3/4 of the slots still in live tiles (and free two tiles or more), they are moved
     // to the leading slots -- every buffer that carries state from round to round, the initial
     // states and the controller state -- so only ceil(active / 32) tiles stay live.  The captured
-    // round reads the same buffers, which keep their addresses.  restoreOrder() puts every
-    // instance back in its own slot when the solve ends.
-    void maybeCompact(int active) {
-        if (!from_ || !batched_) return;
+    // round reads the same buffers, which keep their addresses, and from then on the rounds run
+    // with grids over the leading slots only (graphFor: one captured round per power-of-two count
+    // of tiles), so stopped tiles cost no CTAs.  restoreOrder() puts every instance back in its
+    // own slot when the solve ends.
+    bool maybeCompact(int active) {
+        if (!from_ || !batched_) return false;
         const long need = ((long)active + kTileB - 1) / kTileB * kTileB;
-        if (4 * (long)active > 3 * capacity_ || capacity_ - need < 2 * kTileB) return;
+        if (4 * (long)active > 3 * capacity_ || capacity_ - need < 2 * kTileB) return false;
         std::vector<int> st((size_t)B_);
         CK(cudaMemcpyAsync(st.data(), S_.status, sizeof(int) * (size_t)B_, cudaMemcpyDeviceToHost, stream_));
         CK(cudaStreamSynchronize(stream_));
@@ -1652,6 +1704,7 @@ private:
         permute(from);
         capacity_ = need;
         compactions_++;
+        return true;
     }
 
     void restoreOrder() {
@@ -1693,15 +1746,52 @@ private:
         CK(cudaStreamSynchronize(stream_));
     }
 
-    void ensureGraph() {
-        if (graph_) return;
-        autotune();
+    // Instances the round's grids cover: the whole batch, or (after an instance compaction) the
+    // leading slots that can still hold running instances, rounded up to a power of two of tiles.
+    long gB() const { return gridB_ > 0 ? gridB_ : B_; }
+    long levelFor(long capacity) const {
+        long tiles = 1;
+        while (tiles * kTileB < capacity) tiles *= 2;
+        return std::min<long>(B_, tiles * kTileB);
+    }
+    // The round for grids over the first `gridB` slots (captured once per level).
+    cudaGraphExec_t graphFor(long gridB) {
+        ensureGraph();
+        if (gridB >= B_) return graph_;
+        auto it = graphsLive_.find(gridB);
+        if (it != graphsLive_.end()) return it->second;
         cudaGraph_t g;
+        gridB_ = gridB;
         CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
         roundSpock();
         CK(cudaStreamEndCapture(stream_, &g));
-        CK(cudaGraphInstantiate(&graph_, g, 0));
+        gridB_ = 0;
+        cudaGraphExec_t e;
+        CK(cudaGraphInstantiate(&e, g, 0));
         CK(cudaGraphDestroy(g));
+        graphsLive_[gridB] = e;
+        return e;
+    }
+    void dropGraphs() {
+        if (graph_) CK(cudaGraphExecDestroy(graph_));
+        graph_ = nullptr;
+        for (auto &kv : graphsLive_) CK(cudaGraphExecDestroy(kv.second));
+        graphsLive_.clear();
+    }
+
+    // The round captured once as a CUDA graph; the template stays, so that a group of solvers
+    // can run their rounds as one graph (spock_solve_group).
+    void ensureGraph() {
+        if (graph_) return;
+        autotune();
+        if (graphTemplate_) {
+            CK(cudaGraphDestroy(graphTemplate_));
+            graphTemplate_ = nullptr;
+        }
+        CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+        roundSpock();
+        CK(cudaStreamEndCapture(stream_, &graphTemplate_));
+        CK(cudaGraphInstantiate(&graph_, graphTemplate_, 0));
     }
 
     int activeCount(std::chrono::steady_clock::time_point t0) {

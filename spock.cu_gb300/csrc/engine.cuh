@@ -87,6 +87,14 @@ public:
     virtual void setIterate(const double *z, long count) = 0;           // host warm start, count*sZ
     virtual void zeroIterate() = 0;
     virtual int run(Algo algo, bool warm) = 0;  // returns number of rounds
+    // A SPOCK solve driven from outside, for a group of solvers whose rounds run as one CUDA graph:
+    // groupBegin sets the solve up (synchronously); roundGraph is the solver's captured round
+    // (owned by the solver); statusDevice its per-instance status (-1 while running); groupEnd
+    // records the rounds it took.
+    virtual void groupBegin(bool warm) = 0;
+    virtual cudaGraph_t roundGraph() = 0;
+    virtual const int *statusDevice() const = 0;
+    virtual void groupEnd(long rounds) = 0;
     virtual void getIterate(long inst, double *out) = 0;
     virtual void getIterates(double *out) = 0;  // all, instance-major count*sZ
     virtual void getFirstInputs(double *out) = 0;  // unscaled u_0, B*nu
@@ -98,7 +106,10 @@ public:
     virtual void cpStep(const double *x0, const double *z, double *cand) = 0;
     virtual void applyM(const double *z, double *mz) = 0;
     virtual void dualOf(const double *prim, double *dual) = 0;
-    // Learned warm start: iterate = mean + basis coef' on the device (FP32 solvers), where basis
+    // The round's reductions (k_reduce) for residual r and M r (instance 0, empty Anderson memory):
+    // out3 = {r'Mr, max|Mr|, r'r} summed over the partials in FP64.
+    virtual void reduceCheck(const double *r, const double *mr, double *out3) = 0;
+    // Learned warm start: iterate = mean + basis coef' on the device (FP32 accumulation), where basis
     // is sZ x k and coef batch x k, BF16 row-major, k a multiple of 64 (tcgen05 GEMM).
     virtual void warmStartPca(const void *basis, const void *coef, int k, const float *mean) = 0;
     virtual int precisionBits() const = 0;

@@ -938,9 +938,9 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, kOpCtasPerSm<T>) k_lop_b(c
 //  1. warps 0..U-1 form rhs = u_i - sum_j B_j' q_j, while the x blocks (on the warps after them,
 //     wrapping round) accumulate sum_j (A_j + B_j K_j)' P_j q_j, which does not depend on d;
 //  2. d = (I + sum B'PB)^-1 rhs: FP32 multiplies by the inverse, precomputed in FP64 from the
-//     cached Cholesky factor and kept as a float pair hi + lo, with Dot2 accumulation (so the
-//     solve is a product on U warps instead of a serial triangular solve on one, and is more
-//     accurate than a float triangular solve); FP64 keeps the reference's triangular solves;
+//     cached Cholesky factor and kept as a float pair hi + lo (so the solve is a product on U
+//     warps instead of a serial triangular solve on one); FP64 keeps the reference's triangular
+//     solves;
 //  3. the x blocks add sum_j A_j'P_j B_j d + K_i'(d - u_i) and write q_i - x_i.
 // ------------------------------------------------------------------------------------------
 template <typename T, bool GM>
@@ -1057,16 +1057,16 @@ __global__ void __launch_bounds__(kTileB *kTileWarps, 2) k_dyn_back_b(const DevP
         T *sd2 = dOwn ? sdOwn : sq;
         const T *dv = kInverse ? sd2 : sd;
         if (kInverse) {
-            for (int task = warp; task < U; task += kTileWarps) {  // d = (Rinv_hi + Rinv_lo) rhs, Dot2
+            for (int task = warp; task < U; task += kTileWarps) {  // d = Rinv_hi rhs + Rinv_lo rhs
                 T a[kRT], cm[kRT];
 #pragma unroll
                 for (int t = 0; t < kRT; t++) a[t] = cm[t] = T(0);
-                gemvcTask(a, cm, sL, nu, nu, task, [&](int k) { return sd[k * kTileB + lane]; });
+                gemvTask(a, sL, nu, nu, task, [&](int k) { return sd[k * kTileB + lane]; });
                 gemvTask(cm, sLlo, nu, nu, task, [&](int k) { return sd[k * kTileB + lane]; });
 #pragma unroll
                 for (int t = 0; t < kRT; t++) {
                     const int r = task * kRT + t;
-                    if (r < nu) sd2[r * kTileB + lane] = finishc(a[t], cm[t], T(0));
+                    if (r < nu) sd2[r * kTileB + lane] = a[t] + cm[t];
                 }
             }
         } else if (warp == 0) {  // (I + sum B'PB) d = rhs with the cached lower Cholesky factor

@@ -193,6 +193,7 @@ __global__ void __launch_bounds__(kGThreads, 1)
                 if (col >= N) break;
                 float v = E.alpha * __uint_as_float(r[q]) + ra + (E.colAdd ? E.colAdd[col] : 0.f);
                 if (E.D) E.D[(size_t)row * E.ldd + col] = v;
+                if (E.D64) E.D64[(size_t)row * E.ldd + col] = (double)v;
                 if (E.gelu) v = geluTanhF(v);
                 if (E.Dact) E.Dact[(size_t)row * E.ldd + col] = v;
                 if (E.Dbf) E.Dbf[(size_t)row * E.lddBf + col] = __float2bfloat16_rn(v);

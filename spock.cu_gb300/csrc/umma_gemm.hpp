@@ -12,6 +12,7 @@ struct GemmEpilogue {
     const float *colAdd = nullptr;  // [N], added to every column n (or null)
     int gelu = 0;                   // GELU (tanh form) after the additions, for Dact and Dbf
     float *D = nullptr;             // FP32 row-major M x N before the GELU, leading dimension ldd (or null)
+    double *D64 = nullptr;          // the same in FP64 (or null)
     float *Dact = nullptr;          // FP32 after the GELU, same layout (or null)
     long ldd = 0;
     __nv_bfloat16 *Dbf = nullptr;   // BF16 copy of the (activated) result, leading dimension lddBf (or null)

@@ -91,6 +91,7 @@ _SIGS = {
     "spock_resolve_device": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _ip, _lp]),
     "spock_project_dynamics_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     "spock_get_dual": (ctypes.c_int, [_vp, _dp, _dp]),
+    "spock_reduce_check": (ctypes.c_int, [_vp, _dp, _dp, _dp]),
     "spock_gemm_bf16": (ctypes.c_int, [_vp, _vp, ctypes.c_long, ctypes.c_long, ctypes.c_int, ctypes.c_float, _vp, _vp,
                                        ctypes.c_int, _vp, _vp, ctypes.c_long, ctypes.c_int]),
     "spock_warm_start_pca": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, _vp]),

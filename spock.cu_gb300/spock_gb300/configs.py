@@ -82,11 +82,12 @@ def config2(path, seed=0, count=1, nx=50, nu=20, horizon=10, stopping=4, states=
     return path, rng.uniform(-1., 1., size=(count, nx))
 
 
-def config3(path, seed=0, count=1, nx=100, nu=40, horizon=8, stopping=3, events=5, radius=2., ball=True):
+def config3(path, seed=0, count=1, nx=100, nu=40, horizon=8, stopping=3, events=5, radius=2., ball=True, cost_scale=1.):
     """Box |x| <= 3 on the states and the input ball ||u||_2 <= 2 (RectangleInputBall); the ball
     needs equal input scales, so this problem is not preconditioned.  With ball=False the input
     constraint is the box |u_i| <= radius instead (Rectangle, preconditioned): the variant the
-    reference's constraint types can express."""
+    reference's constraint types can express.  `cost_scale` multiplies every cost term, as in
+    config2."""
     rng = np.random.default_rng(seed)
     tree = F.IidProcess(np.ones(events) / events, horizon=horizon, stopping_stage=stopping).build()
     dyn = _stable_dynamics(rng, nx, nu, events)
@@ -102,29 +103,51 @@ def config3(path, seed=0, count=1, nx=100, nu=40, horizon=8, stopping=3, events=
      .with_constraint_leaf(F.Rectangle(-3. * np.ones(nx), 3. * np.ones(nx)))
      .with_risk(F.AVaR(.9))
      .with_preconditioning(not ball)
+     .with_cost_scaling(cost_scale)
      .generate_problem(path))
     return path, rng.uniform(-1., 1., size=(count, nx))
 
 
+def _mixed_spec(root, seed, k, nx_range, states_range, horizon_range, stopping_range):
+    rng = np.random.default_rng([seed, k])
+    nx = int(rng.integers(nx_range[0], nx_range[1] + 1))
+    states = int(rng.integers(states_range[0], states_range[1] + 1))
+    horizon = int(rng.integers(horizon_range[0], horizon_range[1] + 1))
+    stopping = int(min(rng.integers(stopping_range[0], stopping_range[1] + 1), horizon - 1))
+    sub = int(rng.integers(0, 2 ** 31))
+    path = os.path.join(root, f"config4_mixed_s{seed}", f"p{k:04d}", "")
+    return path, dict(seed=sub, nx=nx, nu=max(1, nx // 2), horizon=horizon, stopping=stopping, states=states), \
+        rng.uniform(-1., 1., size=nx)
+
+
+def _mixed_write(job):
+    path, kw, cost_scale = job
+    if not os.path.exists(os.path.join(path, "data.json")):
+        config2(path, cost_scale=cost_scale, **kw)
+    return path
+
+
 def config4_mixed(root, seed=0, count=256, nx_range=(8, 96), states_range=(2, 4), horizon_range=(5, 15),
-                  stopping_range=(2, 4), cost_scale=1e-3):
+                  stopping_range=(2, 4), cost_scale=1e-3, workers=1):
     """Write `count` problems under root/config4_mixed_s{seed}/p{k}/ (each kept if already there);
-    returns [(path, x0)] with one initial state (nx,) per problem.  The ranges are inclusive."""
+    returns [(path, x0)] with one initial state (nx,) per problem.  The ranges are inclusive.
+    With workers > 1 the problems are written by a pool of processes (started by spawn)."""
     import json
+    specs = [_mixed_spec(root, seed, k, nx_range, states_range, horizon_range, stopping_range) for k in range(count)]
+    jobs = [(path, kw, cost_scale) for path, kw, _ in specs]
+    if workers > 1:
+        import multiprocessing as mp
+        for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):  # one BLAS thread a worker
+            os.environ.setdefault(var, "1")
+        with mp.get_context("spawn").Pool(workers) as pool:
+            pool.map(_mixed_write, jobs)
+    else:
+        for j in jobs:
+            _mixed_write(j)
     out = []
-    for k in range(count):
-        rng = np.random.default_rng([seed, k])
-        nx = int(rng.integers(nx_range[0], nx_range[1] + 1))
-        states = int(rng.integers(states_range[0], states_range[1] + 1))
-        horizon = int(rng.integers(horizon_range[0], horizon_range[1] + 1))
-        stopping = int(min(rng.integers(stopping_range[0], stopping_range[1] + 1), horizon - 1))
-        sub = int(rng.integers(0, 2 ** 31))
-        path = os.path.join(root, f"config4_mixed_s{seed}", f"p{k:04d}", "")
-        if not os.path.exists(os.path.join(path, "data.json")):
-            config2(path, seed=sub, nx=nx, nu=max(1, nx // 2), horizon=horizon, stopping=stopping, states=states,
-                    cost_scale=cost_scale)
-        assert json.load(open(os.path.join(path, "data.json")))["numStates"] == nx
-        out.append((path, rng.uniform(-1., 1., size=nx)))
+    for path, kw, x0 in specs:
+        assert json.load(open(os.path.join(path, "data.json")))["numStates"] == kw["nx"]
+        out.append((path, x0))
     return out
 
 

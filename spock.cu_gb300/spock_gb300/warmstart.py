@@ -6,9 +6,13 @@ generated; the predicted iterate mean + basis @ coefficients is handed to the so
 (spock_set_iterate_device) and every instance is then solved to the same tolerance as a cold
 start, so the warm start changes the iteration count, never the answer.
 
-The MLP's forward, backward and Adam kernels are the library's own (csrc/mlp.cu, spock_mlp_*).
-The PCA basis is computed once, offline, with a randomized range finder whose products are plain
-library GEMMs (torch.matmul) and an SVD of the small projected matrix.
+The MLP's forward, backward and Adam kernels are the library's own (csrc/mlp.cu, spock_mlp_*),
+all products on the tcgen05 tensor cores.  The reconstruction mean + basis coef' is the
+library's tensor-core GEMM as well (spock_warm_start_pca), writing the solver's iterate directly;
+basis and coefficients enter as BF16 hi + lo pairs (three K segments), so the reconstructed
+iterate is accurate to about FP32.  The PCA basis itself is computed once, offline, with a
+randomized range finder whose products are plain library GEMMs (torch.matmul) and an SVD of the
+small projected matrix.
 """
 import ctypes
 
@@ -80,6 +84,11 @@ class PcaMlpWarmStart:
 
     def fit(self, x0s, zs, epochs=200, batch=1024, lr=1e-3, oversample=32, log=None):
         """x0s: (N, nx) numpy; zs: (N, size) torch float32 CUDA tensor of solutions."""
+        self.fit_basis(zs, oversample)
+        return self.fit_mlp(x0s, self.project(zs), epochs, batch, lr, log)
+
+    def fit_basis(self, zs, oversample=32):
+        """Mean and k-dimensional PCA basis of solutions zs ((N, size) torch float32, CUDA)."""
         import torch
         dev = zs.device
         self.mean = zs.mean(0)
@@ -90,7 +99,18 @@ class PcaMlpWarmStart:
         Q, _ = torch.linalg.qr(Y)
         _, S, Vt = torch.linalg.svd(Zc @ Q, full_matrices=False)
         self.basis = (Q @ Vt.T)[:, :self.k].contiguous()     # (size, k), orthonormal columns
-        coef = Zc @ self.basis                               # (N, k)
+        self.explained = float((S[:self.k] ** 2).sum() / (S ** 2).sum())
+        self._bop = None
+
+    def project(self, zs):
+        """(N, k) coefficients of solutions zs in the basis."""
+        return (zs - self.mean) @ self.basis
+
+    def fit_mlp(self, x0s, coef, epochs=200, batch=1024, lr=1e-3, log=None):
+        """Train the MLP x0 -> coefficients (coef: (N, k) torch float32, CUDA)."""
+        import torch
+        dev = coef.device
+        g = torch.Generator(device=dev).manual_seed(self.seed + 1)
         self.cscale = coef.std(0).clamp_min(1e-12)
         self.xs_mean = torch.tensor(x0s.mean(0), dtype=torch.float32, device=dev)
         self.xs_std = torch.tensor(x0s.std(0) + 1e-12, dtype=torch.float32, device=dev)
@@ -106,17 +126,40 @@ class PcaMlpWarmStart:
                 losses.append(self.mlp.train_step(X[idx], T[idx], lr))
             if log and (ep % max(1, epochs // 10) == 0 or ep == epochs - 1):
                 log(f"epoch {ep}: loss {losses[-1]:.4e}")
-        self.explained = float((S[:self.k] ** 2).sum() / (S ** 2).sum())
         return losses
 
-    def predict(self, x0s):
-        """(B, size) torch float32 predicted iterates for x0s (numpy (B, nx))."""
+    def coefficients(self, x0s):
+        """(B, k) torch float32 predicted basis coefficients for x0s (numpy (B, nx))."""
         import torch
         X = (torch.tensor(x0s, dtype=torch.float32, device=self.mean.device) - self.xs_mean) / self.xs_std
-        coef = self.mlp.forward(X) * self.cscale
-        return self.mean + coef @ self.basis.T
+        return self.mlp.forward(X) * self.cscale
+
+    def predict(self, x0s):
+        """(B, size) torch float32 predicted iterates (a host-side check of warm_start)."""
+        return self.mean + self.coefficients(x0s) @ self.basis.T
+
+    def _basis_operand(self):
+        """basis as a BF16 [hi | lo | hi] operand (size x 3 kP, kP = k padded to 64), built once."""
+        import torch
+        if getattr(self, "_bop", None) is None:
+            kP = (self.k + 63) // 64 * 64
+            hi = self.basis.to(torch.bfloat16)
+            lo = (self.basis - hi.float()).to(torch.bfloat16)
+            op = torch.zeros(self.basis.shape[0], 3 * kP, dtype=torch.bfloat16, device=self.basis.device)
+            op[:, :self.k], op[:, kP:kP + self.k], op[:, 2 * kP:2 * kP + self.k] = hi, lo, hi
+            self._bop, self._kP = op.contiguous(), kP
+        return self._bop, self._kP
 
     def warm_start(self, cache, x0s):
-        """Put the predicted iterates into `cache` (batch = len(x0s)); then call resolveBatch(x0s)."""
-        z = self.predict(x0s).T.contiguous()                 # element-major: size x batch
-        cache.setIterateDevice(z.data_ptr(), 32)
+        """Put the predicted iterates into `cache` (batch = len(x0s)) with the library's tensor-core
+        GEMM; then call resolveBatch(x0s)."""
+        import torch
+        bop, kP = self._basis_operand()
+        c = self.coefficients(x0s)
+        hi = c.to(torch.bfloat16)
+        lo = (c - hi.float()).to(torch.bfloat16)
+        cop = torch.zeros(c.shape[0], 3 * kP, dtype=torch.bfloat16, device=c.device)
+        cop[:, :self.k], cop[:, kP:kP + self.k], cop[:, 2 * kP:2 * kP + self.k] = hi, hi, lo
+        mean = self.mean.float().contiguous()
+        _check(lib().spock_warm_start_pca(cache._h, ctypes.c_void_p(bop.data_ptr()), ctypes.c_void_p(cop.data_ptr()),
+                                          3 * kP, ctypes.c_void_p(mean.data_ptr())))

@@ -193,3 +193,8 @@ def test_config4_mixed(oracle_lib, tmp_path):
     assert len(sizes) > 1
     again = configs.config4_mixed(str(tmp_path), seed=1, **kw)
     assert all(a[0] == b[0] and np.array_equal(a[1], b[1]) for a, b in zip(probs, again))
+    # written by a pool of two processes: the same files
+    par = configs.config4_mixed(str(tmp_path / "pool"), seed=1, workers=2, **kw)
+    for (a, xa), (b, xb) in zip(probs, par):
+        assert np.array_equal(xa, xb)
+        assert open(a + "dynamics_AB_d.bt", "rb").read() == open(b + "dynamics_AB_d.bt", "rb").read()

@@ -326,10 +326,12 @@ def test_fp64_polish_of_fp32_solve(oracle_lib):
     t2, d2, c64 = make(path, 64, batch=32, tol=1e-9, max_iters=20000)
     assert (c64.polish(c32, x0s) == 0).all()
     u0 = c64.firstInputs()
+    oS = P.size_prim - P.n  # the optimal cost: s at the root
     for b in (0, 31):
         z, s = P.run(x0s[b], oracle_lib.options(tol=1e-9, max_iters=20000), "spock")
         u_ref = P.states_inputs(z)[1][:P.nu]
         assert np.abs(u0[b] - u_ref).max() <= 1e-6 * max(1., np.abs(u_ref).max()), b
+        assert abs(c64.solution(b)[oS] - z[oS]) <= 1e-6 * abs(z[oS]), b
 
 
 @pytest.mark.parametrize("batch", [1, 32])

@@ -16,6 +16,8 @@ import pytest
 
 from test_gpu_parity import make, rel
 
+import spock_gb300 as sg
+
 pytestmark = pytest.mark.gpu
 
 
@@ -64,3 +66,53 @@ def test_fp32_projection_error_against_fp64(oracle_lib, tmp_problems):
     err_gpu = np.abs(gpu - ref).max() / np.abs(ref).max()
     print(f"FP32 projection error vs FP64: GPU {err_gpu:.3g}, emulated plain float {err_plain:.3g}")
     assert err_gpu < 0.75 * err_plain, (err_gpu, err_plain)
+
+
+@pytest.mark.parametrize("batch", [1, 64])
+def test_fp32_round_reductions_against_fp64(oracle_lib, tmp_problems, batch):
+    """The round's reductions of an FP32 solver (k_reduce: blocks of 32 rows summed in float,
+    running sums as float pairs, partials widened to FP64) on a config-2 sized residual
+    (138,760 entries): r'Mr, max|Mr| and r'r against FP64 sums of the same float-rounded
+    vectors, to 1e-6 relative."""
+    from spock_gb300 import configs
+    path, _ = configs.cached("config2", tmp_problems, seed=0, count=1, cost_scale=1e-3)
+    P = oracle_lib.Problem(path)
+    t, d, c = make(path, 32, batch=batch)
+    rng = np.random.default_rng(6)
+    r = (rng.standard_normal(P.size) * np.exp(rng.uniform(-3, 3, P.size))).astype(np.float32).astype(np.float64)
+    mr = (r + 0.3 * rng.standard_normal(P.size)).astype(np.float32).astype(np.float64)
+    out = np.zeros(3)
+    from spock_gb300 import _p
+    assert sg.lib().spock_reduce_check(c._h, _p(r), _p(mr), _p(out)) == 0, sg.lib().spock_last_error()
+    ref = np.array([r @ mr, np.abs(mr).max(), r @ r])
+    assert out[1] == ref[1]
+    assert abs(out[0] - ref[0]) <= 1e-6 * np.abs(r * mr).sum()
+    assert abs(out[2] - ref[2]) <= 1e-6 * ref[2]
+
+
+def test_fp32_bench_workload_against_fp64_oracle(oracle_lib, tmp_problems):
+    """The benchmark's step on its problem (config 2, costs x 1e-3): 32 instances at the FP64
+    oracle's cold solutions are re-solved after an x0 disturbance U[-0.05, 0.05]^50 to tol(1e-4),
+    by the FP32 batched solver on the GPU and by the FP64 oracle from the same starting point.
+    Both converge; the GPU's optimal costs s_0 are within 1e-2 (relative) and its first inputs u_0
+    within 1e-2 of the oracle's -- two stopping points of the same iteration at the same
+    tolerance, in FP32 and FP64 (the benchmark line reports the measured errors as fp64_error)."""
+    from spock_gb300 import configs
+    path, x0 = configs.cached("config2", tmp_problems, seed=0, count=32, cost_scale=1e-3)
+    P = oracle_lib.Problem(path)
+    opts = oracle_lib.options(tol=1e-4, anderson=5, max_iters=20000)
+    z0 = np.zeros((32, P.size))
+    _, st, _, _, _ = P.solve_many_warm(x0, z0, opts, 16, warm=False)
+    assert (st == 0).all()
+    x1 = np.clip(x0 + np.random.default_rng(3).uniform(-.05, .05, x0.shape), -1, 1)
+    zr = z0.copy()
+    _, st, _, _, _ = P.solve_many_warm(x1, zr, opts, 16, warm=True)
+    assert (st == 0).all()
+    t, d, c = make(path, 32, batch=32, tol=1e-4, max_iters=20000, anderson=5)
+    assert (c.runSpockBatch(x1, prev=z0) == 0).all()
+    oS = P.size_prim - P.n
+    zg = c.solutions()
+    cost_err = np.abs(zg[:, oS] - zr[:, oS]) / np.abs(zr[:, oS])
+    ug, ur = zg[:, :P.nu] / P.scaling[P.nx:P.nx + P.nu], zr[:, :P.nu] / P.scaling[P.nx:P.nx + P.nu]
+    print(f"FP32 vs FP64 at tol(1e-4): cost {cost_err.max():.3g} (max), u0 {np.abs(ug - ur).max():.3g} (max)")
+    assert cost_err.max() <= 1e-2 and np.abs(ug - ur).max() <= 1e-2
