@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--train-tol", type=float, default=1e-4, help="warmstart: tolerance of the training solves")
     ap.add_argument("--test", type=int, default=10240, help="warmstart: held-out initial states")
     ap.add_argument("--epochs", type=int, default=40, help="warmstart: MLP training epochs")
+    ap.add_argument("--variants", default="ball,box", help="precision: config-3 input constraints to run (ball, box)")
     ap.add_argument("--kernels", help="instead of the benchmark line: comma-separated round kernels (lstar, lop, "
                                       "mlstar, mlop, dyn, reduce, update, round) timed one launch at a time on a "
                                       "random iterate of --batch instances, tiles 1 per CTA (profiling driver)")
@@ -513,7 +514,7 @@ def study_precision(args):
     sg.build()
     oracle.build()
     n, B = 8, 32
-    for ball in (True, False):
+    for ball in [v == "ball" for v in args.variants.split(",")]:
         path, x0 = configs.cached("config3", PROBLEM_DIR, seed=args.seed, count=n, ball=ball, cost_scale=COST_SCALE)
         xb = np.resize(x0, (B, x0.shape[1]))
         t = sg.ScenarioTree(path)
