@@ -241,10 +241,11 @@ def fp64_cold_gpu(path, x0s, device, count, max_iters):
             "note": "cold FP64 solves stop at tol(1e-4)'s relative tolerance (about 1e-3 here)"}
 
 
-# DRAM bytes (read + write) of one launch of a kernel, from an ncu capture (dram__bytes_read.sum +
-# dram__bytes_write.sum) of this workload: {(kernel, batch): bytes}.  The bench reports it as
-# roofline.traffic when the dominant kernel and batch have an entry.
-TRAFFIC_BYTES = {}
+# DRAM bytes (read + write) of one launch of a kernel (the dynamics sweep: of one sweep), from an
+# ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of this workload at 256 instances,
+# scaled to 1,024 by the instances (node matrices counted once): {(kernel, batch): bytes}.  The
+# bench reports it as roofline.traffic when the dominant kernel and batch have an entry.
+TRAFFIC_BYTES = {("dyn", 1024): 666e6, ("update", 1024): 8.90e9, ("reduce", 1024): 4.57e9}
 
 
 def fp64_error(z_gpu, z_ref, nu, scaling_u, size_prim, nodes):

@@ -117,7 +117,9 @@ __global__ void __launch_bounds__(kGThreads, 1)
     uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(bars + 2 * kGStages + 1);
     __shared__ int sFail;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * kGM, n0 = blockIdx.y * kGN;
+    // x runs over the column tiles: the CTAs that share a 128-row slice of A run together, so A is
+    // read from DRAM about once (B, the smaller operand, stays in L2)
+    const int m0 = blockIdx.y * kGM, n0 = blockIdx.x * kGN;
     const int kBlocks = K / kGK;
     auto full = [&](int s) { return sAddr(bars + s); };
     auto empty = [&](int s) { return sAddr(bars + kGStages + s); };
@@ -246,12 +248,12 @@ void gemmBf16(const void *A, const void *B, long M, long N, int K, const GemmEpi
     if (M < 1 || N < 1 || K < kGK || K % kGK)
         throw std::invalid_argument("[gemm] sizes must be positive and K a multiple of 64");
     if (((uintptr_t)A | (uintptr_t)B) & 15) throw std::invalid_argument("[gemm] operands must be 16-byte aligned");
-    if (M > (1L << 30) || N > 65535L * kGN) throw std::invalid_argument("[gemm] problem too large");
+    if (M > 65535L * kGM || N > (1L << 30)) throw std::invalid_argument("[gemm] problem too large");
     if (!E.err) throw std::invalid_argument("[gemm] an error flag is required");
     static std::once_flag attr;
     std::call_once(attr, [] { cudaFuncSetAttribute(k_umma_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem); });
     const CUtensorMap ta = tensorMap(A, M, K), tb = tensorMap(B, N, K);
-    const dim3 grid((unsigned)((M + kGM - 1) / kGM), (unsigned)((N + kGN - 1) / kGN));
+    const dim3 grid((unsigned)((N + kGN - 1) / kGN), (unsigned)((M + kGM - 1) / kGM));
     k_umma_gemm<<<grid, kGThreads, kGemmSmem, stream>>>(ta, tb, (int)M, (int)N, K, E);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) throw std::runtime_error(std::string("[gemm] launch: ") + cudaGetErrorString(e));
