@@ -75,6 +75,16 @@ int spock_problem_step(spock_problem p, double *step, double *scaling_or_null);
 int spock_offline_dynamics(spock_problem p, int device, int replace, double *P, double *K, double *lowChol,
                            double *ABKTr, double *APB);
 
+/* Complete a data folder whose problem data is written but whose offline cache is not: the
+ * GPU half of the reference's Problem constructor (api/python/spock/problem.py:192-231, 402-417),
+ * all in FP64 on GPU `device`.  It reads the folder (cache files may be absent, stepSize may be
+ * 0), computes the dynamics cache, the AVaR nullspace projectors I - S'(SS')^-1 S and the step
+ * size 0.99 / ||L|| (power iteration with the library's L and L*: at most `iters` steps, stopped
+ * once the estimate is steady to 1e-14), and writes dynamics_P, _K, _lowCholesky, _ABKTr, _APB,
+ * risk_NNtr (with the folder's _d or _f suffix) and data.json's stepSize.  *step (may be NULL)
+ * receives the step size. */
+int spock_offline_complete(const char *path, int device, int iters, double *step);
+
 /* CacheBuilder<T>(tree, data)...build() (src/cache.cuh:1215-1244). */
 int spock_solver_create(spock_problem p, const spock_options *opts, spock_solver *out);
 void spock_solver_free(spock_solver s);

@@ -57,6 +57,23 @@ spock_solver_s *solver(spock_solver s) {
     need(s, "solver");
     return s;
 }
+
+// Take over a freshly computed dynamics cache, with Pe = P e per node for affine dynamics
+// (dynamics.cuh:236).
+void adoptCache(spock::HostProblem &hp, const spock::OfflineCache &c) {
+    hp.P = c.P;
+    hp.K = c.K;
+    hp.lowChol = c.lowChol;
+    hp.ABKTr = c.ABKTr;
+    hp.APB = c.APB;
+    if (hp.affine) {
+        const long n = hp.numNodes, nx = hp.nx;
+        hp.Pe.assign((size_t)(nx * n), 0.);
+        for (long j = 0; j < n; j++)
+            for (long col = 0; col < nx; col++)
+                for (long r = 0; r < nx; r++) hp.Pe[j * nx + r] += hp.P[j * nx * nx + col * nx + r] * hp.e[j * nx + col];
+    }
+}
 }  // namespace
 
 extern "C" {
@@ -179,21 +196,27 @@ int spock_offline_dynamics(spock_problem pp, int device, int replace, double *P,
         put(c.lowChol, lowChol);
         put(c.ABKTr, ABKTr);
         put(c.APB, APB);
-        if (replace) {
-            hp.P = c.P;
-            hp.K = c.K;
-            hp.lowChol = c.lowChol;
-            hp.ABKTr = c.ABKTr;
-            hp.APB = c.APB;
-            if (hp.affine) {  // Pe = P e per node (dynamics.cuh:236)
-                const long n = hp.numNodes, nx = hp.nx;
-                hp.Pe.assign((size_t)(nx * n), 0.);
-                for (long j = 0; j < n; j++)
-                    for (long col = 0; col < nx; col++)
-                        for (long r = 0; r < nx; r++)
-                            hp.Pe[j * nx + r] += hp.P[j * nx * nx + col * nx + r] * hp.e[j * nx + col];
-            }
-        }
+        if (replace) adoptCache(hp, c);
+    });
+}
+
+int spock_offline_complete(const char *path, int device, int iters, double *step) {
+    return guard([&] {
+        need(path, "path");
+        if (iters < 1) throw std::invalid_argument("[offlineComplete] iters must be positive");
+        spock::HostProblem hp = spock::HostProblem::load(path, true);
+        adoptCache(hp, spock::offlineDynamicsGpu(hp, device));
+        hp.NNtr = spock::offlineNullspaceGpu(hp, device);
+        // ||L||^2 does not depend on the step size; the engine wants a positive one to start
+        if (!(hp.stepSize > 0)) hp.stepSize = 1.;
+        spock::Options opt;
+        std::unique_ptr<spock::EngineBase> eng(spock::makeEngine(hp, opt, 1, 64, device));
+        const double lam = eng->normLsq(iters, 1e-14);
+        eng.reset();
+        if (!(lam > 0)) throw std::invalid_argument("[offlineComplete] ||L|| is zero");
+        hp.stepSize = 0.99 / std::sqrt(lam);
+        spock::writeOfflineCache(hp);
+        if (step) *step = hp.stepSize;
     });
 }
 

@@ -892,7 +892,7 @@ public:
         downloadSlice(MR_, mz, 0, D_.sZ);
     }
 
-    double normLsq(int iters) override {  // problem.py:402-417 computes the same with ARPACK
+    double normLsq(int iters, double rtol) override {  // problem.py:402-417 computes the same with ARPACK
         allLive();
         const size_t np = (size_t)D_.sPrim * B_;
         fill(W1_, (size_t)D_.sZ * B_, T(0));
@@ -911,6 +911,7 @@ public:
         };
         nrm2 = norm2();
         k_scale<T><<<(int)std::min<size_t>((np + 255) / 256, 152 * 8), 256, 0, stream_>>>(W1_, np, 1. / std::sqrt(nrm2));
+        int steady = 0;
         for (int it = 0; it < iters; it++) {
             OpArgs<T> A = blankArgs();
             A.in1 = W1_; A.a1 = 1; A.cL = 1; A.out = W2_;  // W2 dual = L p
@@ -919,8 +920,11 @@ public:
             A2.in1 = W2_; A2.a1 = 1; A2.cL = 1; A2.out = W1_;  // W1 prim = L* L p
             launchLstar<2>(A2);
             nrm2 = norm2();
+            const double prev = lam;
             lam = std::sqrt(nrm2);  // ||L* L p|| with ||p|| = 1
             if (!(lam > 0)) break;
+            steady = std::fabs(lam - prev) <= rtol * lam ? steady + 1 : 0;
+            if (rtol > 0 && steady >= 20) break;
             k_scale<T><<<(int)std::min<size_t>((np + 255) / 256, 152 * 8), 256, 0, stream_>>>(W1_, np, 1. / lam);
             CK(cudaGetLastError());
         }

@@ -129,9 +129,11 @@ public:
     // Override the tuner: tiles per CTA of L*, L and the dynamics sweep (1, 2, 4 or 8), double
     // buffering where more than one tile fits twice in shared memory.
     virtual void setTuning(int lstar, int lop, int dyn) = 0;
-    // ||L||^2 = lambda_max(L* L) by `iters` steps of the power iteration on the device, with the
-    // solver's own L and L* kernels (instance 0); the step size is 0.99 / sqrt of it.
-    virtual double normLsq(int iters) = 0;
+    // ||L||^2 = lambda_max(L* L) by at most `iters` steps of the power iteration on the device,
+    // with the solver's own L and L* kernels (instance 0); the step size is 0.99 / sqrt of it.
+    // With rtol > 0 it stops once the estimate changed by at most rtol (relative) in each of
+    // 20 consecutive steps.
+    virtual double normLsq(int iters, double rtol = 0.) = 0;
     long lastRounds() const { return lastRounds_; }
     long lastCompactions() const { return lastCompactions_; }
     int device() const { return device_; }

@@ -1,4 +1,5 @@
-// Offline cache of the dynamics projection, computed on the GPU in FP64.
+// Offline cache of the dynamics projection and the AVaR nullspace projectors, computed on the
+// GPU in FP64.
 //
 // The reference builds it in numpy when it generates a problem (problem.py:192-213), from the
 // leaves to the root: with P_j = I at the leaves, for every nonleaf node i and its children j
@@ -10,6 +11,13 @@
 // stage; every product is a loop of FP64 dot products spread over the CTA's threads, with the
 // node's intermediates in a global scratch area (any nx, nu).  All matrices are column-major
 // per node, the layout of the .bt files the problem loader reads.
+//
+// The AVaR kernel projection reads, for every nonleaf node i with m children, the orthogonal
+// projector onto ker S_i of the padded matrix S_i = [E_i' -I -I] (problem.py:215-231, 263-267,
+// with E = [alpha I; -I; 1'] from build.py:1184-1193): row j of S_i (m x (4E+1)) holds alpha in
+// column j, -1 in column m + j, 1 in column 2m, -1 in columns 2E+1+j and 3E+1+j.  The reference
+// takes an SVD nullspace basis N and stores N N'; the same projector is I - S'(SS')^-1 S, which
+// one CTA per node forms here with a Cholesky factor of the m x m Gram matrix.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -143,6 +151,69 @@ __global__ void k_offline_stage(const OfflineArgs a) {
     }
 }
 
+// One CTA per nonleaf node; shared memory S (m x nd, row-major), the Gram factor (m x m) and
+// W = (SS')^-1 S (m x nd), with m <= E.
+__global__ void k_offline_nullspace(const long *numCh, int E, int nd, double alpha, double *NNtr, int *fail) {
+    extern __shared__ double sh[];
+    const int i = blockIdx.x, m = (int)numCh[i], yd = 2 * E + 1;
+    double *S = sh, *G = S + (size_t)E * nd, *W = G + (size_t)E * E;
+    for (int e = threadIdx.x; e < m * nd; e += blockDim.x) S[e] = 0.;
+    __syncthreads();
+    for (int j = threadIdx.x; j < m; j += blockDim.x) {
+        S[j * nd + j] = alpha;
+        S[j * nd + m + j] = -1.;
+        S[j * nd + 2 * m] = 1.;
+        S[j * nd + yd + j] = -1.;
+        S[j * nd + yd + E + j] = -1.;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {  // G = S S'
+        const int r = e % m, c = e / m;
+        double s = 0.;
+        for (int k = 0; k < nd; k++) s += S[r * nd + k] * S[c * nd + k];
+        G[c * m + r] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {  // lower Cholesky factor in place (column-major, lower triangle)
+        for (int c = 0; c < m; c++) {
+            double d = G[c * m + c];
+            for (int k = 0; k < c; k++) d -= G[k * m + c] * G[k * m + c];
+            if (!(d > 0.)) {
+                *fail = 1;
+                d = 1.;
+            }
+            d = sqrt(d);
+            G[c * m + c] = d;
+            for (int r = c + 1; r < m; r++) {
+                double s = G[c * m + r];
+                for (int k = 0; k < c; k++) s -= G[k * m + r] * G[k * m + c];
+                G[c * m + r] = s / d;
+            }
+        }
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < nd; c += blockDim.x) {  // W(:, c) = G^-1 S(:, c)
+        for (int r = 0; r < m; r++) {
+            double s = S[r * nd + c];
+            for (int q = 0; q < r; q++) s -= G[q * m + r] * W[q * nd + c];
+            W[r * nd + c] = s / G[r * m + r];
+        }
+        for (int r = m - 1; r >= 0; r--) {
+            double s = W[r * nd + c];
+            for (int q = r + 1; q < m; q++) s -= G[r * m + q] * W[q * nd + c];
+            W[r * nd + c] = s / G[r * m + r];
+        }
+    }
+    __syncthreads();
+    double *out = NNtr + (size_t)i * nd * nd;
+    for (int e = threadIdx.x; e < nd * nd; e += blockDim.x) {  // I - S' W, column-major
+        const int r = e % nd, c = e / nd;
+        double s = r == c ? 1. : 0.;
+        for (int j = 0; j < m; j++) s -= S[j * nd + r] * W[j * nd + c];
+        out[e] = s;
+    }
+}
+
 template <typename V>
 double *upload(const V &v) {
     double *d = nullptr;
@@ -208,6 +279,35 @@ OfflineCache offlineDynamicsGpu(const HostProblem &p, int device) {
                       (void *)a.APB, (void *)a.scratch, (void *)dFail})
         cudaFree(ptr);
     if (fail) throw std::invalid_argument("[offlineDynamics] I + sum B'PB is not positive definite");
+    return out;
+}
+
+std::vector<double> offlineNullspaceGpu(const HostProblem &p, int device) {
+    const int E = (int)p.numEvents, nd = (int)p.nullDim;
+    const long nnl = p.numNonleaf;
+    if (nd != 4 * E + 1) throw std::invalid_argument("[offlineNullspace] rowsNNtr must be 4 numEvents + 1");
+    const size_t smem = sizeof(double) * (2 * (size_t)E * nd + (size_t)E * E);
+    if (smem > 200 * 1024) throw std::invalid_argument("[offlineNullspace] too many events for one CTA");
+    OCK(cudaSetDevice(device));
+    OCK(cudaFuncSetAttribute(k_offline_nullspace, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    std::vector<long> numCh(p.numChildren.begin(), p.numChildren.end());
+    long *dNum = nullptr;
+    double *dOut = nullptr;
+    int *dFail = nullptr;
+    OCK(cudaMalloc(&dNum, sizeof(long) * numCh.size()));
+    OCK(cudaMalloc(&dOut, sizeof(double) * (size_t)nd * nd * nnl));
+    OCK(cudaMalloc(&dFail, sizeof(int)));
+    OCK(cudaMemcpy(dNum, numCh.data(), sizeof(long) * numCh.size(), cudaMemcpyHostToDevice));
+    OCK(cudaMemset(dFail, 0, sizeof(int)));
+    k_offline_nullspace<<<(unsigned)nnl, 128, smem>>>(dNum, E, nd, p.alpha, dOut, dFail);
+    OCK(cudaGetLastError());
+    OCK(cudaDeviceSynchronize());
+    std::vector<double> out((size_t)nd * nd * nnl);
+    int fail = 0;
+    OCK(cudaMemcpy(out.data(), dOut, sizeof(double) * out.size(), cudaMemcpyDeviceToHost));
+    OCK(cudaMemcpy(&fail, dFail, sizeof(int), cudaMemcpyDeviceToHost));
+    for (void *ptr : {(void *)dNum, (void *)dOut, (void *)dFail}) cudaFree(ptr);
+    if (fail) throw std::invalid_argument("[offlineNullspace] S S' is not positive definite");
     return out;
 }
 

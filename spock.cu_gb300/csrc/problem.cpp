@@ -1,9 +1,11 @@
 // Data-folder loader for HostProblem (see problem.hpp for the format references).
 #include "problem.hpp"
 
+#include <cctype>
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <fstream>
 #include <limits>
@@ -242,7 +244,7 @@ void loadConstraint(HostProblem &p, const std::string &dir, bool leaf) {
 
 double HostProblem::minScaling() const { return *std::min_element(scaling.begin(), scaling.end()); }
 
-HostProblem HostProblem::load(const std::string &folder) {
+HostProblem HostProblem::load(const std::string &folder, bool withoutCache) {
     HostProblem p;
     std::string dir = folder;
     if (!dir.empty() && dir.back() != '/') dir += '/';
@@ -275,7 +277,8 @@ HostProblem HostProblem::load(const std::string &folder) {
     p.alpha = js.kv.count("risk.alpha") ? js.number("risk.alpha") : 1.;
     if (p.numNodes < 2 || p.numNonleaf < 1 || p.numStages < 2 || p.nx < 1 || p.nu < 1 || p.numEvents < 1)
         fail("[Tree] invalid sizes in data.json");
-    if (!(p.stepSize > 0)) fail("[Problem] stepSize must be positive");
+    if (!(p.stepSize > 0) && !(withoutCache && p.stepSize == 0)) fail("[Problem] stepSize must be positive");
+    p.dtype = exists(dir + "dynamics_AB_d.bt") ? 'd' : 'f';
 
     const long n = p.numNodes, nnl = p.numNonleaf, nx = p.nx, nu = p.nu;
     p.stages = readIndex(dir, "stages");
@@ -300,11 +303,17 @@ HostProblem HostProblem::load(const std::string &folder) {
 
     p.BTr = expect(readTensor(dir, "dynamics_BTr"), nu * nx * n, "dynamics_BTr");
     p.AB = expect(readTensor(dir, "dynamics_AB"), nx * (nx + nu) * n, "dynamics_AB");
-    p.K = expect(readTensor(dir, "dynamics_K"), nu * nx * nnl, "dynamics_K");
-    p.ABKTr = expect(readTensor(dir, "dynamics_ABKTr"), nx * nx * n, "dynamics_ABKTr");
-    p.P = expect(readTensor(dir, "dynamics_P"), nx * nx * n, "dynamics_P");
-    p.APB = expect(readTensor(dir, "dynamics_APB"), nx * nu * n, "dynamics_APB");
-    p.lowChol = expect(readTensor(dir, "dynamics_lowCholesky"), nu * nu * nnl, "dynamics_lowCholesky");
+    // the offline cache: zeros in place of files not yet written when withoutCache is set
+    auto cache = [&](const std::string &name, long count) {
+        if (withoutCache && !exists(dir + name + "_d.bt") && !exists(dir + name + "_f.bt"))
+            return std::vector<double>((size_t)count, 0.);
+        return expect(readTensor(dir, name), count, name);
+    };
+    p.K = cache("dynamics_K", nu * nx * nnl);
+    p.ABKTr = cache("dynamics_ABKTr", nx * nx * n);
+    p.P = cache("dynamics_P", nx * nx * n);
+    p.APB = cache("dynamics_APB", nx * nu * n);
+    p.lowChol = cache("dynamics_lowCholesky", nu * nu * nnl);
     if (p.affine) {
         p.e = expect(readTensor(dir, "dynamics_c"), nx * n, "dynamics_c");
         p.Pe.assign(nx * n, 0.);  // Pe = P e per node (dynamics.cuh:236)
@@ -332,7 +341,7 @@ HostProblem HostProblem::load(const std::string &folder) {
     }
     loadConstraint(p, dir, false);
     loadConstraint(p, dir, true);
-    p.NNtr = expect(readTensor(dir, "risk_NNtr"), p.nullDim * p.nullDim * nnl, "risk_NNtr");
+    p.NNtr = cache("risk_NNtr", p.nullDim * p.nullDim * nnl);
     p.b = expect(readTensor(dir, "risk_b"), p.yDim * nnl, "risk_b");
     if (p.preconditioned) p.scaling = expect(readTensor(dir, "scaling"), nx + nu, "scaling");
     else p.scaling.assign(nx + nu, 1.);
@@ -355,6 +364,57 @@ HostProblem HostProblem::load(const std::string &folder) {
     p.sizeVI = p.dimVI * p.numLeaf;
     p.sizeDual = p.sizeI + p.sizeII + p.sizeIII + p.sizeIV + p.sizeV + p.sizeVI;
     return p;
+}
+
+namespace {
+
+void writeTensor(const std::string &dir, const std::string &name, char dt, const std::vector<double> &v,
+                 uint64_t rows, uint64_t cols, uint64_t mats) {
+    if ((size_t)(rows * cols * mats) != v.size()) fail("[" + name + "] size does not match its dims");
+    const std::string fn = dir + name + "_" + dt + ".bt";
+    std::ofstream f(fn, std::ios::binary | std::ios::trunc);
+    if (!f) fail("cannot write " + fn);
+    const uint64_t h[3] = {rows, cols, mats};
+    f.write(reinterpret_cast<const char *>(h), sizeof h);
+    if (dt == 'd') {
+        f.write(reinterpret_cast<const char *>(v.data()), (std::streamsize)(v.size() * sizeof(double)));
+    } else {
+        std::vector<float> w(v.begin(), v.end());
+        f.write(reinterpret_cast<const char *>(w.data()), (std::streamsize)(w.size() * sizeof(float)));
+    }
+    if (!f) fail("cannot write " + fn);
+}
+
+}  // namespace
+
+void writeOfflineCache(const HostProblem &p) {
+    const std::string &dir = p.path;
+    const uint64_t n = p.numNodes, nnl = p.numNonleaf, nx = p.nx, nu = p.nu, nd = p.nullDim;
+    writeTensor(dir, "dynamics_P", p.dtype, p.P, nx, nx, n);
+    writeTensor(dir, "dynamics_K", p.dtype, p.K, nu, nx, nnl);
+    writeTensor(dir, "dynamics_lowCholesky", p.dtype, p.lowChol, nu, nu, nnl);
+    writeTensor(dir, "dynamics_ABKTr", p.dtype, p.ABKTr, nx, nx, n);
+    writeTensor(dir, "dynamics_APB", p.dtype, p.APB, nx, nu, n);
+    writeTensor(dir, "risk_NNtr", p.dtype, p.NNtr, nd, nd, nnl);
+    // data.json: replace the value of "stepSize" in place
+    const std::string fn = dir + "data.json";
+    auto raw = slurp(fn);
+    std::string text(raw.begin(), raw.end());
+    size_t k = text.find("\"stepSize\"");
+    if (k == std::string::npos) fail("[data.json] missing key 'stepSize'");
+    k = text.find(':', k);
+    if (k == std::string::npos) fail("[data.json] malformed stepSize");
+    size_t a = k + 1;
+    while (a < text.size() && std::isspace((unsigned char)text[a])) a++;
+    size_t b = a;
+    while (b < text.size() && text[b] != ',' && text[b] != '}' && !std::isspace((unsigned char)text[b])) b++;
+    char num[64];
+    std::snprintf(num, sizeof num, "%.17g", p.stepSize);
+    text.replace(a, b - a, num);
+    std::ofstream f(fn, std::ios::binary | std::ios::trunc);
+    if (!f) fail("cannot write " + fn);
+    f << text;
+    if (!f) fail("cannot write " + fn);
 }
 
 }  // namespace spock

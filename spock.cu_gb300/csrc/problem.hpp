@@ -25,6 +25,7 @@ enum ConstraintKind {
 
 struct HostProblem {
     std::string path;
+    char dtype = 'd';  // suffix of the folder's floating-point tensors: 'd' (FP64) or 'f' (FP32)
     // tree (tree.cuh:48-76)
     long numEvents = 0, numNodes = 0, numNonleaf = 0, numLeaf = 0, numStages = 0;
     long nx = 0, nu = 0;
@@ -53,9 +54,17 @@ struct HostProblem {
     long sizeI = 0, sizeII = 0, sizeIII = 0, sizeIV = 0, sizeV = 0, sizeVI = 0, sizeDual = 0;
     long dimIV = 0, dimVI = 0, dimIII = 0, dimV = 0;  // per-node block sizes
 
-    static HostProblem load(const std::string &folder);  // throws std::invalid_argument
+    // Throws std::invalid_argument.  With withoutCache the offline cache (dynamics_P, _K,
+    // _lowCholesky, _ABKTr, _APB, risk_NNtr) may be absent and is then zero, and stepSize may be
+    // zero: the state of a folder whose problem data is written and whose cache is not yet.
+    static HostProblem load(const std::string &folder, bool withoutCache = false);
     long sizeIterate() const { return sizePrim + sizeDual; }
     double minScaling() const;
 };
+
+// Write the offline cache of `p` (dynamics_P, _K, _lowCholesky, _ABKTr, _APB, risk_NNtr) into
+// its folder with the folder's own suffix, and set the stepSize of its data.json to p.stepSize
+// (the other keys are kept as they are).
+void writeOfflineCache(const HostProblem &p);
 
 }  // namespace spock

@@ -87,6 +87,7 @@ _SIGS = {
     "spock_mlp_forward": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _vp]),
     "spock_mlp_train_step": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_float, ctypes.POINTER(ctypes.c_float)]),
     "spock_offline_dynamics": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp, _dp]),
+    "spock_offline_complete": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, _dp]),
     "spock_resolve": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.c_long, _ip, _lp]),
     "spock_resolve_device": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _ip, _lp]),
     "spock_project_dynamics_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
@@ -135,6 +136,15 @@ def _check(rc):
 
 def _p(a):
     return a.ctypes.data_as(_dp)
+
+
+def offline_complete(path, device=0, iters=20000):
+    """Write the offline cache of a data folder whose problem data is written: the dynamics cache,
+    the AVaR nullspace projectors and the step size, computed on GPU `device` in FP64
+    (problem.py:192-231, 402-417).  Returns the step size."""
+    step = ctypes.c_double()
+    _check(lib().spock_offline_complete(os.path.join(path, "").encode(), int(device), int(iters), ctypes.byref(step)))
+    return step.value
 
 
 class ScenarioTree:

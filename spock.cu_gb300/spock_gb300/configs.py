@@ -61,7 +61,7 @@ def config1(path, seed=0, count=1):
     return path, rng.uniform(-1., 1., size=(count, nx))
 
 
-def config2(path, seed=0, count=1, nx=50, nu=20, horizon=10, stopping=4, states=3, cost_scale=1.):
+def config2(path, seed=0, count=1, nx=50, nu=20, horizon=10, stopping=4, states=3, cost_scale=1., offline="host"):
     rng = np.random.default_rng(seed)
     P = rng.dirichlet(np.ones(states), size=states)
     tree = F.MarkovChain(P, np.ones(states) / states, horizon=horizon, stopping_stage=stopping).build()
@@ -78,16 +78,17 @@ def config2(path, seed=0, count=1, nx=50, nu=20, horizon=10, stopping=4, states=
      .with_constraint_leaf(F.Rectangle(-3. * np.ones(nx), 3. * np.ones(nx)))
      .with_risk(F.AVaR(.95))
      .with_cost_scaling(cost_scale)
-     .generate_problem(path))
+     .generate_problem(path, offline=offline))
     return path, rng.uniform(-1., 1., size=(count, nx))
 
 
-def config3(path, seed=0, count=1, nx=100, nu=40, horizon=8, stopping=3, events=5, radius=2., ball=True, cost_scale=1.):
+def config3(path, seed=0, count=1, nx=100, nu=40, horizon=8, stopping=3, events=5, radius=2., ball=True, cost_scale=1.,
+            offline="host"):
     """Box |x| <= 3 on the states and the input ball ||u||_2 <= 2 (RectangleInputBall); the ball
     needs equal input scales, so this problem is not preconditioned.  With ball=False the input
     constraint is the box |u_i| <= radius instead (Rectangle, preconditioned): the variant the
     reference's constraint types can express.  `cost_scale` multiplies every cost term, as in
-    config2."""
+    config2.  offline="gpu" computes the offline cache on the GPU (Factory.generate_problem)."""
     rng = np.random.default_rng(seed)
     tree = F.IidProcess(np.ones(events) / events, horizon=horizon, stopping_stage=stopping).build()
     dyn = _stable_dynamics(rng, nx, nu, events)
@@ -104,7 +105,7 @@ def config3(path, seed=0, count=1, nx=100, nu=40, horizon=8, stopping=3, events=
      .with_risk(F.AVaR(.9))
      .with_preconditioning(not ball)
      .with_cost_scaling(cost_scale)
-     .generate_problem(path))
+     .generate_problem(path, offline=offline))
     return path, rng.uniform(-1., 1., size=(count, nx))
 
 

@@ -149,6 +149,8 @@ class IidProcess:
         self.d = np.asarray(distribution, dtype=np.float64).ravel()
         self.N = int(horizon)
         self.tau = int(horizon if stopping_stage is None else stopping_stage)
+        if self.tau > self.N:
+            raise ValueError("stopping time greater than number of stages")
         if abs(self.d.sum() - 1) >= 1e-10 or (self.d <= 1e-16).any():
             raise ValueError("invalid distribution")
 
@@ -333,15 +335,21 @@ class Factory:
         self.cost_scale = float(factor)
         return self
 
-    def generate_problem(self, path, dt="d", step_size=None):
+    def generate_problem(self, path, dt="d", step_size=None, offline="host", device=0):
+        """Write the problem to `path`.  offline="host" computes the offline cache here in numpy
+        (dynamics cache, nullspace projectors, ARPACK step size); offline="gpu" writes the
+        problem data only and has the library compute the cache on GPU `device` in FP64
+        (`spock_offline_complete`), as the C++ generator does."""
+        if offline not in ("host", "gpu"):
+            raise ValueError("offline must be 'host' or 'gpu'")
+        f = self
         if self.cost_scale != 1.:
             import copy
             f = copy.copy(self)
             f.cost_events = [_scale_cost(c, self.cost_scale) for c in self.cost_events]
             f.leaf_cost = _scale_cost(self.leaf_cost, self.cost_scale)
             f.cost_scale = 1.
-            return Problem(f, path, dt, step_size)
-        return Problem(self, path, dt, step_size)
+        return Problem(f, path, dt, step_size, gpu_device=device if offline == "gpu" else None)
 
 
 def _scale_cost(cost, factor):
@@ -357,7 +365,7 @@ def _scale_cost(cost, factor):
 class Problem:
     """Problem data + offline cache, written to `path` (problem.py:16-687)."""
 
-    def __init__(self, f, path, dt="d", step_size=None):
+    def __init__(self, f, path, dt="d", step_size=None, gpu_device=None):
         t, nx, nu = f.tree, f.nx, f.nu
         self.tree, self.nx, self.nu = t, nx, nu
         n, nnl = t.num_nodes, t.num_nonleaf_nodes
@@ -470,12 +478,25 @@ class Problem:
         self.null_dim = 4 * E + 1
         self.y_dim = 2 * E + 1
         self.b = np.zeros((nnl, self.y_dim))
-        self.nntr = np.zeros((nnl, self.null_dim, self.null_dim))
         for i in range(nnl):
             ch = t.children[i]
             m = len(ch)
             self.b[i, :m] = t.cond_prob[ch]
             self.b[i, 2 * m] = 1.
+        self._sizes()
+        self.path = path
+        if gpu_device is not None:
+            self._write(path, dt, with_cache=False)
+            from . import offline_complete
+            gpu_step = offline_complete(path, gpu_device)
+            self.step_size = float(step_size) if step_size is not None else gpu_step
+            if step_size is not None:
+                self._write_step_size(path)
+            self._read_cache(path, dt)
+            return
+        self.nntr = np.zeros((nnl, self.null_dim, self.null_dim))
+        for i in range(nnl):
+            m = len(t.children[i])
             S = np.zeros((m, self.null_dim))
             S[np.arange(m), np.arange(m)] = self.alpha
             S[np.arange(m), m + np.arange(m)] = -1.
@@ -484,10 +505,21 @@ class Problem:
             S[np.arange(m), self.y_dim + E + np.arange(m)] = -1.
             self.nntr[i] = np.eye(self.null_dim) - S.T @ np.linalg.solve(S @ S.T, S)
         self._offline_dynamics()
-        self._sizes()
         self.step_size = float(step_size) if step_size is not None else self._step_size()
-        self.path = path
         self._write(path, dt)
+
+    def _read_cache(self, path, dt):
+        """The offline cache as the GPU wrote it, in this object's (mats, rows, cols) layout."""
+        get = lambda name: np.transpose(read_bt(os.path.join(path, name + "_" + dt + ".bt")), (2, 0, 1))
+        self.P, self.K, self.lowChol = get("dynamics_P"), get("dynamics_K"), get("dynamics_lowCholesky")
+        self.ABKTr, self.APB, self.nntr = get("dynamics_ABKTr"), get("dynamics_APB"), get("risk_NNtr")
+
+    def _write_step_size(self, path):
+        fn = os.path.join(path, "data.json")
+        meta = json.load(open(fn))
+        meta["stepSize"] = float(self.step_size)
+        with open(fn, "w") as fh:
+            json.dump(meta, fh, indent=1)
 
     @staticmethod
     def _con_data(con, scale):
@@ -677,7 +709,9 @@ class Problem:
         return .99 / np.sqrt(lam)
 
     # -- files
-    def _write(self, path, dt):
+    def _write(self, path, dt, with_cache=True):
+        """The folder; with_cache=False leaves out the offline cache and writes stepSize 0 (the
+        input of spock_offline_complete)."""
         os.makedirs(path, exist_ok=True)
         t, nx, nu = self.tree, self.nx, self.nu
         fdt = _np_dt(dt)
@@ -688,14 +722,16 @@ class Problem:
         AB = np.concatenate((self.A, self.B), axis=2)
         w("dynamics_BTr", stack(np.transpose(self.B, (0, 2, 1))))
         w("dynamics_AB", stack(AB))
-        w("dynamics_P", stack(self.P))
-        w("dynamics_K", stack(self.K))
-        w("dynamics_ABKTr", stack(self.ABKTr))
-        w("dynamics_APB", stack(self.APB))
-        w("dynamics_lowCholesky", stack(self.lowChol))
+        if with_cache:
+            w("dynamics_P", stack(self.P))
+            w("dynamics_K", stack(self.K))
+            w("dynamics_ABKTr", stack(self.ABKTr))
+            w("dynamics_APB", stack(self.APB))
+            w("dynamics_lowCholesky", stack(self.lowChol))
         if self.affine:
             w("dynamics_c", stack(self.c[:, :, None]))
-        w("risk_NNtr", stack(self.nntr))
+        if with_cache:
+            w("risk_NNtr", stack(self.nntr))
         w("risk_b", stack(self.b[:, :, None]))
         if self.preconditioned:
             w("scaling", self.scaling)
@@ -738,7 +774,8 @@ class Problem:
             "constraint": {"nonleaf": self.nl_con.kind, "leaf": self.l_con.kind},
             "risk": {"type": "avar", "alpha": self.alpha},
             "rowsS2": int(t.num_events), "rowsNNtr": int(self.null_dim),
-            "stepSize": float(self.step_size), "preconditioned": bool(self.preconditioned),
+            "stepSize": float(self.step_size) if with_cache else 0.,
+            "preconditioned": bool(self.preconditioned),
         }
         with open(os.path.join(path, "data.json"), "w") as fh:
             json.dump(meta, fh, indent=1)
