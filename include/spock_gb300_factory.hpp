@@ -301,6 +301,7 @@ class MarkovChain {
    public:
     MarkovChain(const Matrix &P, std::vector<double> v, long horizon, long stopping = -1)
         : P_(P), v_(std::move(v)), N_(horizon), tau_(stopping < 0 ? horizon : stopping) {
+        if (N_ < 1 || tau_ < 1) detail::fail("horizon and stopping stage must be at least 1");
         if (tau_ > N_) detail::fail("stopping time greater than number of stages");
         if (P_.rows != P_.cols || P_.rows != (long)v_.size()) detail::fail("[MarkovChain] dimension mismatch");
         auto check = [](const std::vector<double> &p) {
@@ -355,6 +356,7 @@ class IidProcess {
    public:
     IidProcess(std::vector<double> d, long horizon, long stopping = -1)
         : d_(std::move(d)), N_(horizon), tau_(stopping < 0 ? horizon : stopping) {
+        if (N_ < 1 || tau_ < 1) detail::fail("horizon and stopping stage must be at least 1");
         if (tau_ > N_) detail::fail("stopping time greater than number of stages");
         double s = 0.;
         for (double x : d_) {

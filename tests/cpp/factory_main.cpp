@@ -95,6 +95,7 @@ int bad(const std::string &which) {
         if (which == "markov") MarkovChain(P, {.5, .5}, 3).build();
         if (which == "iid") IidProcess({.5, .4}, 3).build();
         if (which == "stopping") IidProcess({.5, .5}, 3, 4).build();
+        if (which == "horizon") MarkovChain(Matrix::identity(2), {.5, .5}, 0).build();
         if (which == "alpha") AVaR(1.5);
         if (which == "rectangle") Constraint::rectangle({1., 0.}, {0., 1.});
         if (which == "leafcost") {

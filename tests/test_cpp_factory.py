@@ -184,7 +184,7 @@ def test_cpp_problem_data_matches_python_factory(exe, tmp_path, case):
     assert step_cpp == 0.
 
 
-@pytest.mark.parametrize("case", ["markov", "iid", "stopping", "alpha", "rectangle", "leafcost"])
+@pytest.mark.parametrize("case", ["markov", "iid", "stopping", "horizon", "alpha", "rectangle", "leafcost"])
 def test_cpp_factory_rejects_invalid_input(exe, case):
     r = subprocess.run([exe, "bad", case], capture_output=True, text=True)
     assert r.returncode == 0 and r.stdout.startswith("invalid_argument"), r.stdout + r.stderr

@@ -68,3 +68,30 @@ def test_no_alloc_rejects_batched_solver():
     c = sg.CacheBuilder(t, d).batch(2).build()
     rc = sg.lib().spock_project_dynamics_noalloc(c._h, ctypes.c_void_p(1), ctypes.c_void_p(1), None)
     assert rc == 1 and b"batch 1" in sg.lib().spock_last_error()
+
+
+def test_no_alloc_projection_in_a_captured_graph():
+    """The call on a capturing stream launches without waiting, so it can be recorded into a
+    CUDA graph; replaying the graph gives the same projection as a direct call."""
+    torch = pytest.importorskip("torch")
+    t, d, c = _solver("cfg1", 64)
+    nx, nu, n, nnl = t.numStates(), t.numInputs(), t.numNodes(), t.numNonleafNodes()
+    head = nu * nnl + nx * n
+    x0s = torch.tensor(golden("cfg1", "initialState_d.bt") * d.scaling()[:nx], dtype=torch.float64, device="cuda")
+    z = torch.tensor(3 * np.random.default_rng(5).standard_normal(head), dtype=torch.float64, device="cuda")
+    direct = z.clone()
+    call = lambda buf, stream: sg.lib().spock_project_dynamics_noalloc(
+        c._h, ctypes.c_void_p(x0s.data_ptr()), ctypes.c_void_p(buf.data_ptr()), stream)
+    assert call(direct, None) == 0, sg.lib().spock_last_error().decode()
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    buf = torch.empty_like(z)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=side):
+        rc = call(buf, ctypes.c_void_p(side.cuda_stream))
+    assert rc == 0, sg.lib().spock_last_error().decode()
+    for _ in range(2):
+        buf.copy_(z)
+        g.replay()
+        torch.cuda.synchronize()
+        assert torch.equal(buf, direct)
