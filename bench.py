@@ -49,9 +49,13 @@ def parse():
     ap.add_argument("--max-iters", type=int, default=20000)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-fp64-baseline", action="store_true", help="skip the plain FP64 SPOCK solves on the GPU")
-    ap.add_argument("--study", choices=["warmstart", "precision", "mixed"],
+    ap.add_argument("--fp64-finish", type=int, default=0,
+                    help="rounds after which the last <= 32 running instances of a step finish in FP64 (0: never)")
+    ap.add_argument("--study", choices=["warmstart", "precision", "mixed", "finish"],
                     help="instead of the benchmark line: the learned warm start (config 5), the precision study "
-                         "(config 3) or the mixed batch (config 4 mixed); one JSON line per result")
+                         "(config 3), the mixed batch (config 4 mixed) or the FP64 finish thresholds "
+                         "(--finish-rounds) on the benchmark's steps; one JSON line per result")
+    ap.add_argument("--finish-rounds", default="0,400,800,1600", help="finish: FP64-finish thresholds to time")
     ap.add_argument("--train", type=int, default=16384, help="warmstart: training solves")
     ap.add_argument("--pca-rows", type=int, default=8192, help="warmstart: solutions the PCA basis is fitted on")
     ap.add_argument("--train-tol", type=float, default=1e-4, help="warmstart: tolerance of the training solves")
@@ -104,12 +108,15 @@ def trajectory(x0s, steps, seed, rank=0):
     return out
 
 
-def config_dict(batch, world):
+def config_dict(batch, world, finish=0):
+    prec = "fp32 iteration, fp64 controller and reductions"
+    if finish > 0:
+        prec += f"; after {finish} rounds the last <= 32 running instances finish in fp64"
     return {"workload": "config4-uniform: %d instances of config2 (Markov 3 states, N=10, stopping 4, 607 nodes, "
                         "nx=50, nu=20, quadratic-plus-linear costs x 1e-3, box |x|<=3 |u|<=1, AVaR 0.95); step = "
                         "warm-started re-solve of every instance after an x0 disturbance U[-0.05,0.05]^50, "
                         "tol(1e-4), Anderson memory 5" % batch,
-            "instances_per_gpu": batch, "precision": "fp32 iteration, fp64 controller and reductions",
+            "instances_per_gpu": batch, "precision": prec, "fp64_finish_rounds": finish,
             "cost_scale": COST_SCALE, "tolerance": "CacheBuilder::tol(1e-4): absolute and relative",
             "l2": "inputs larger than L2 (per-step working set ~10 GB)", "parallelism": f"replicas x{world}"}
 
@@ -279,6 +286,8 @@ def run_gpu(args):
         return (sg.CacheBuilder(tree, data).tol(TOL).andersonBuffer(ANDERSON).maxIters(args.max_iters)
                 .precision(32).batch(B).device(local).build())
     cache = fp32_cache()
+    if args.fp64_finish > 0:
+        cache.fp64Finish(args.fp64_finish)
     snap = fp32_cache()  # holds the iterate the timed steps start from, for the end-to-end replay
     nx, nu = tree.numStates(), tree.numInputs()
     extra = 2  # untimed steps after the timed ones: GPU against the FP64 oracle on the same re-solves
@@ -386,7 +395,7 @@ def run_gpu(args):
         out = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-               "config": config_dict(B, world), "e2e": e2e,
+               "config": config_dict(B, world, args.fp64_finish), "e2e": e2e,
                "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
                             "kernel_ms": kms, "algorithmic_bytes": kbytes,
@@ -656,6 +665,60 @@ def study_mixed(args):
                           iters_max=int(it_seq.max()), same_iterations=bool((it_seq == it_group).all()))), flush=True)
 
 
+def study_finish(args):
+    """The FP64 finish (spock_set_fp64_finish) on the benchmark's workload: from the same warm-up
+    state, the K timed re-solve steps are run once per threshold in --finish-rounds (0: FP32
+    throughout).  Per threshold: device-timed solves/s, rounds per step, outer iterations, and the
+    largest relative difference of the optimal costs s_0 from the FP32-throughout run."""
+    import torch
+    import spock_gb300 as sg
+    torch.cuda.set_device(0)
+    sg.build()
+    B = args.batch
+    path, x0s = workload(args.seed, B)
+    tree = sg.ScenarioTree(path)
+    data = sg.ProblemData(tree)
+    make = lambda: (sg.CacheBuilder(tree, data).tol(TOL).andersonBuffer(ANDERSON).maxIters(args.max_iters)
+                    .precision(32).batch(B).build())
+    cache, snap = make(), make()
+    traj = trajectory(x0s, args.warmup + args.steps, args.seed)
+    x_dev = [torch.tensor(x.T.copy(), dtype=torch.float32, device="cuda").contiguous() for x in traj]
+    cache.runSpockBatch(x0s)
+    for k in range(args.warmup):
+        cache.resolveDevice(x_dev[k].data_ptr())
+    snap.copyIterateFrom(cache)
+    oS = tree.numNonleafNodes() * (tree.numInputs() + 2 * tree.numEvents() + 1) + tree.numNodes() * (
+        tree.numStates() + 2) - tree.numNodes()
+    base = None
+    for R in [int(v) for v in args.finish_rounds.split(",")]:
+        cache.copyIterateFrom(snap)
+        cache.fp64Finish(R)
+        if R > 0:  # the FP64 solver is made on first use: once, outside the timed steps
+            cache.resolveDevice(x_dev[args.warmup].data_ptr())
+            cache.copyIterateFrom(snap)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        conv, its, rounds = 0, [], 0
+        for k in range(args.steps):
+            st = cache.resolveDevice(x_dev[args.warmup + k].data_ptr())
+            conv += int((st == 0).sum())
+            its.append(cache.countersAll()[:, 6].copy())
+            rounds += cache.runStats()[0]
+        e1.record()
+        torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) / 1e3
+        cost = cache.solutions()[:, oS]
+        if base is None:
+            base = cost
+        its = np.concatenate(its)
+        print(json.dumps({"study": "finish", "fp64_finish_rounds": R, "solves_per_s": B * args.steps / sec,
+                          "converged": conv, "instances": B * args.steps, "rounds_per_step": rounds / args.steps,
+                          "outer_iterations": {"mean": float(its.mean()), "max": int(its.max())},
+                          "cost_rel_diff_vs_fp32_max": float(np.max(np.abs(cost - base) / np.abs(base)))}),
+              flush=True)
+
+
 def main():
     args = parse()
     if args.kernels:
@@ -672,6 +735,9 @@ def main():
         return
     if args.study == "precision":
         study_precision(args)
+        return
+    if args.study == "finish":
+        study_finish(args)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -183,6 +183,15 @@ int spock_step_size(spock_solver s, int iters, double *norm_sq, double *step);
  * small-batch kernels.  No reference counterpart. */
 int spock_set_tuning(spock_solver s, const int *in3);
 
+/* FP64 finish of an FP32 batched solver (batch >= 32): once a SPOCK solve has run `rounds`
+ * rounds and at most 32 of its instances are still running, those instances move with their
+ * whole SuperMann state (iterate, Anderson memory, controller state, tolerance) into an FP64
+ * solver of the same problem, made on first use with batch 32, which continues the same
+ * iteration in FP64 until they stop; their final iterates, statuses and counters come back.
+ * rounds = 0 (the default) turns it off.  No effect on FP64 solvers or batches below 32.  No
+ * reference counterpart: the reference iterates in one precision (cache.cuh:1008-1132). */
+int spock_set_fp64_finish(spock_solver s, long rounds);
+
 /* Dynamics projection that allocates no device memory.  No counterpart in the reference: it
  * is for callers that cannot allocate while they solve, such as a control loop re-solving
  * under a hard deadline (a cudaMalloc's latency or failure is not acceptable there) or a host

@@ -183,6 +183,9 @@ class Cache {
         check(spock_reset(h_.get()));
         status_.assign((size_t)batch_, notRun);
     }
+    // FP32 batched solvers: the last <= 32 running instances finish in FP64 after `rounds`
+    // rounds (spock_set_fp64_finish); 0 turns it off.  No reference counterpart.
+    void fp64Finish(size_t rounds) { check(spock_set_fp64_finish(h_.get(), (long)rounds)); }
 
    private:
     template <typename V>

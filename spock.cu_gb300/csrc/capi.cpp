@@ -587,6 +587,10 @@ int spock_step_size(spock_solver sv, int iters, double *norm_sq, double *step) {
     });
 }
 
+int spock_set_fp64_finish(spock_solver sv, long rounds) {
+    return guard([&] { solver(sv)->eng->setFinishDouble(rounds); });
+}
+
 int spock_set_tuning(spock_solver sv, const int *in3) {
     return guard([&] {
         need(in3, "tiles");

@@ -545,6 +545,41 @@ __global__ void k_gather_state(int *__restrict__ id, const int *__restrict__ is,
     for (int q = 0; q < perGamma; q++) dd[a0 + (size_t)s * perGamma + q] = ds[a0 + (size_t)f * perGamma + q];
 }
 
+// FP64 finish: columns of an element-major buffer between two solvers of different batch and
+// precision, dst[k * Bd + dIdx[s]] = src[k * Bs + sIdx[s]] for s < count <= 32 (one warp lane per
+// instance, warps over the rows).
+template <typename TD, typename TS>
+__global__ void k_move_cols(TD *__restrict__ dst, long Bd, const TS *__restrict__ src, long Bs, const int *__restrict__ dIdx,
+                            const int *__restrict__ sIdx, int count, long rows) {
+    const int s = threadIdx.x & 31;
+    if (s >= count) return;
+    const size_t d = (size_t)dIdx[s], f = (size_t)sIdx[s];
+    const long w = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), nw = (long)gridDim.x * (blockDim.x >> 5);
+    for (long k = w; k < rows; k += nw) dst[(size_t)k * Bd + d] = (TD)src[(size_t)k * Bs + f];
+}
+
+// The controller state of instance sIdx[s] of one solver into slot dIdx[s] of another (layouts as
+// in k_gather_state, batches Bs and Bd); s < count.
+__global__ void k_move_state(int *__restrict__ id, long Bd, const int *__restrict__ is, long Bs, double *__restrict__ dd,
+                             const double *__restrict__ ds, const int *__restrict__ dIdx, const int *__restrict__ sIdx,
+                             int count, int nInt, int nDbl, int perG, int perGamma) {
+    const int s = threadIdx.x;
+    if (s >= count) return;
+    const size_t d = (size_t)dIdx[s], f = (size_t)sIdx[s];
+    for (int q = 0; q < nInt; q++) id[(size_t)q * Bd + d] = is[(size_t)q * Bs + f];
+    for (int q = 0; q < nDbl; q++) dd[(size_t)q * Bd + d] = ds[(size_t)q * Bs + f];
+    const size_t gd = (size_t)nDbl * Bd, gs = (size_t)nDbl * Bs;
+    for (int q = 0; q < perG; q++) dd[gd + d * perG + q] = ds[gs + f * perG + q];
+    const size_t ad = gd + (size_t)perG * Bd, as = gs + (size_t)perG * Bs;
+    for (int q = 0; q < perGamma; q++) dd[ad + d * perGamma + q] = ds[as + f * perGamma + q];
+}
+
+// Slots from `from` on hold no instance: mark them stopped so that they change nothing.
+__global__ void k_stop_from(int *status, int from, int B) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= from && b < B) status[b] = 0;
+}
+
 // Measurement helper: put every instance in phase A with an Anderson update pending.
 __global__ void k_force_phaseA(DevState S, int B, int m) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
@@ -594,6 +629,9 @@ __global__ void k_count_active(const int *status, int B, int *out) {
 // ------------------------------------------------------------------------------------------ engine
 template <typename T>
 class Engine final : public EngineBase {
+    template <typename U>
+    friend class Engine;  // the FP64 finish moves state between an FP32 solver and its FP64 twin
+
 public:
     Engine(const HostProblem &hp, const Options &opt, long batch, int device) {
         hp_ = hp;
@@ -709,6 +747,11 @@ public:
         lastSeconds_ = std::chrono::duration<double>(std::chrono::steady_clock::now() - groupT0_).count();
     }
 
+    void setFinishDouble(long rounds) override {
+        if (rounds < 0) throw std::invalid_argument("[fp64Finish] rounds must be >= 0");
+        finishAfter_ = rounds;
+    }
+
     int run(Algo algo, bool warm) override {
         const auto t0 = std::chrono::steady_clock::now();
         beginSolve(algo, warm);
@@ -726,6 +769,13 @@ public:
                     const int act = activeCount(t0);
                     if (act == 0) break;
                     if (maybeCompact(act)) round = graphFor(levelFor(capacity_));
+                    if (finishAfter_ > 0 && rounds >= finishAfter_ && act <= kTileB && sizeof(T) == 4 && batched_) {
+                        long r2 = 0, l2 = 0;
+                        finishInDouble(t0, r2, l2);
+                        rounds += (int)r2;
+                        launches += l2;
+                        break;
+                    }
                 }
             }
             restoreOrder();
@@ -1084,6 +1134,9 @@ private:
     int compactions_ = 0;
     double *part_ = nullptr;
     int *gemmErr_ = nullptr;  // error flag of the tensor-core GEMM (warmStartPca)
+    long finishAfter_ = 0;    // FP64 finish: rounds after which the last tile moves to FP64 (0: never)
+    std::unique_ptr<Engine<double>> twin_;
+    int *twinIdx_ = nullptr;  // slot lists of a move: twin slots, then this solver's slots
     int *hostActive_ = nullptr, *devActive_ = nullptr;
     int chunks_ = 1, nv_ = 0;
     long rowsPerChunk_ = 1;
@@ -1796,6 +1849,88 @@ private:
         roundSpock();
         CK(cudaStreamEndCapture(stream_, &graphTemplate_));
         CK(cudaGraphInstantiate(&graph_, graphTemplate_, 0));
+    }
+
+    // FP64 finish.  The instances still running (at most one tile of 32) move with their whole
+    // SuperMann state -- iterate, previous iterate and residual, backup, direction, Anderson
+    // memory, initial state and controller state -- into an FP64 solver of the same problem
+    // (batch 32, made on first use), which continues the same iteration in FP64 until they
+    // stop; their final iterates and controller state (status, counters) come back converted.
+    // Only the arithmetic of the remaining iterations changes: an FP32 instance that stalls near
+    // the tolerance on float rounding finishes in the FP64 number of iterations.
+    void finishInDouble(std::chrono::steady_clock::time_point t0, long &rounds, long &launches) {
+        if constexpr (sizeof(T) == 4) {
+            std::vector<int> st((size_t)B_);
+            CK(cudaMemcpyAsync(st.data(), S_.status, sizeof(int) * (size_t)B_, cudaMemcpyDeviceToHost, stream_));
+            CK(cudaStreamSynchronize(stream_));
+            std::vector<int> idx;  // [0, count): twin slots; [kTileB, kTileB + count): this solver's slots
+            for (long q = 0; q < B_ && (long)idx.size() < kTileB; q++)
+                if (st[(size_t)q] == -1) idx.push_back((int)q);
+            const int count = (int)idx.size();
+            if (count == 0) return;
+            if (!twin_) {  // made, tuned and captured before any state moves in
+                twin_.reset(new Engine<double>(hp_, opt_, kTileB, device_));
+                twinIdx_ = dalloc<int>(2 * kTileB);
+                twin_->ensureGraph();
+                CK(cudaStreamSynchronize(twin_->stream_));
+            }
+            Engine<double> &tw = *twin_;
+            std::vector<int> both(2 * kTileB, 0);
+            for (int s = 0; s < count; s++) {
+                both[(size_t)s] = s;
+                both[(size_t)(kTileB + s)] = idx[(size_t)s];
+            }
+            CK(cudaMemcpyAsync(twinIdx_, both.data(), sizeof(int) * both.size(), cudaMemcpyHostToDevice, stream_));
+            const int *dTw = twinIdx_, *dMe = twinIdx_ + kTileB;
+            const long nzr = D_.sZ;
+            auto toTwin = [&](double *dst, const T *src, long rows) {
+                const int grid = (int)std::min<long>((rows + 7) / 8, 152 * 8);
+                k_move_cols<double, T><<<grid, 256, 0, stream_>>>(dst, tw.B_, src, B_, dTw, dMe, count, rows);
+                CK(cudaGetLastError());
+            };
+            toTwin(tw.Z_, Z_, nzr);
+            toTwin(tw.PREV_, PREV_, nzr);
+            toTwin(tw.RPREV_, RPREV_, nzr);
+            toTwin(tw.BACKUP_, BACKUP_, nzr);
+            toTwin(tw.DIR_, DIR_, nzr);
+            for (long q = 0; q < opt_.anderson; q++) {
+                toTwin(tw.ANDR_ + (size_t)q * nzr * tw.B_, ANDR_ + (size_t)q * nzr * B_, nzr);
+                toTwin(tw.ANDZ_ + (size_t)q * nzr * tw.B_, ANDZ_ + (size_t)q * nzr * B_, nzr);
+            }
+            toTwin(tw.x0s_, x0s_, D_.nx);
+            const int perG = kMaxAnderson * kMaxAnderson, perGamma = kMaxAnderson;
+            k_move_state<<<1, kTileB, 0, stream_>>>(tw.ib_, tw.B_, ib_, B_, tw.db_, db_, dTw, dMe, count, 16, 8, perG,
+                                                   perGamma);
+            CK(cudaGetLastError());
+            CK(cudaStreamSynchronize(stream_));
+            k_stop_from<<<1, kTileB, 0, tw.stream_>>>(tw.S_.status, count, (int)tw.B_);
+            CK(cudaGetLastError());
+            CK(cudaMemsetAsync(tw.S_.timeUp, 0, sizeof(int), tw.stream_));
+            tw.continueSolve(t0, rounds, launches);
+            // back: the final iterates and the controller state
+            const int grid = (int)std::min<long>((nzr + 7) / 8, 152 * 8);
+            k_move_cols<T, double><<<grid, 256, 0, stream_>>>(Z_, B_, tw.Z_, tw.B_, dMe, dTw, count, nzr);
+            CK(cudaGetLastError());
+            k_move_state<<<1, kTileB, 0, stream_>>>(ib_, B_, tw.ib_, tw.B_, db_, tw.db_, dMe, dTw, count, 16, 8, perG,
+                                                   perGamma);
+            CK(cudaGetLastError());
+            CK(cudaStreamSynchronize(stream_));
+            launches += 2 * (7 + 2 * opt_.anderson) + 4;
+        }
+    }
+
+    // Run rounds on the state already in place (no re-initialisation) until every instance stops.
+    void continueSolve(std::chrono::steady_clock::time_point t0, long &rounds, long &launches) {
+        allLive();
+        capacity_ = B_;
+        cudaGraphExec_t round = graphFor(B_);
+        for (;;) {
+            CK(cudaGraphLaunch(round, stream_));
+            rounds++;
+            launches += launchesPerRound();
+            if (rounds % 10 == 0 && activeCount(t0) == 0) break;
+        }
+        CK(cudaStreamSynchronize(stream_));
     }
 
     int activeCount(std::chrono::steady_clock::time_point t0) {

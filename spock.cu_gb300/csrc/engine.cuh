@@ -91,6 +91,9 @@ public:
     // groupBegin sets the solve up (synchronously); roundGraph is the solver's captured round
     // (owned by the solver); statusDevice its per-instance status (-1 while running); groupEnd
     // records the rounds it took.
+    // FP32 solvers: after `rounds` rounds (0: never), once at most 32 instances are running, they
+    // finish in FP64 (the same iteration continued by an FP64 solver of the same problem).
+    virtual void setFinishDouble(long rounds) = 0;
     virtual void groupBegin(bool warm) = 0;
     virtual cudaGraph_t roundGraph() = 0;
     virtual const int *statusDevice() const = 0;

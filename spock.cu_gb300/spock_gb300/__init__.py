@@ -74,6 +74,7 @@ _SIGS = {
     "spock_tuning": (ctypes.c_int, [_vp, _ip]),
     "spock_counters_all": (ctypes.c_int, [_vp, _lp]),
     "spock_set_tuning": (ctypes.c_int, [_vp, _ip]),
+    "spock_set_fp64_finish": (ctypes.c_int, [_vp, ctypes.c_long]),
     "spock_step_size": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp]),
     "spock_copy_iterate": (ctypes.c_int, [_vp, _vp]),
     "spock_solve_group": (ctypes.c_int, [ctypes.c_long, ctypes.POINTER(_vp), ctypes.c_int, ctypes.POINTER(_dp), _lp,
@@ -445,6 +446,12 @@ class Cache:
         lam, step = ctypes.c_double(), ctypes.c_double()
         _check(lib().spock_step_size(self._h, int(iters), ctypes.byref(lam), ctypes.byref(step)))
         return lam.value, step.value
+
+    def fp64Finish(self, rounds):
+        """FP32 batched solvers: after `rounds` rounds, the last <= 32 running instances continue
+        the same iteration in FP64 (spock_set_fp64_finish); 0 turns it off."""
+        _check(lib().spock_set_fp64_finish(self._h, int(rounds)))
+        return self
 
     def setTuning(self, lstar, lop, dyn):
         """Override the autotuner's tiles per CTA (1, 2, 4 or 8) for L*, L and the dynamics sweep."""

@@ -90,13 +90,11 @@ def test_fp32_round_reductions_against_fp64(oracle_lib, tmp_problems, batch):
     assert abs(out[2] - ref[2]) <= 1e-6 * ref[2]
 
 
-def test_fp32_bench_workload_against_fp64_oracle(oracle_lib, tmp_problems):
-    """The benchmark's step on its problem (config 2, costs x 1e-3): 32 instances at the FP64
-    oracle's cold solutions are re-solved after an x0 disturbance U[-0.05, 0.05]^50 to tol(1e-4),
-    by the FP32 batched solver on the GPU and by the FP64 oracle from the same starting point.
-    Both converge; the GPU's optimal costs s_0 are within 1e-2 (relative) and its first inputs u_0
-    within 1e-2 of the oracle's -- two stopping points of the same iteration at the same
-    tolerance, in FP32 and FP64 (the benchmark line reports the measured errors as fp64_error)."""
+@pytest.fixture(scope="module")
+def bench_resolves(oracle_lib, tmp_problems):
+    """The benchmark problem (config 2, costs x 1e-3), 32 instances at the FP64 oracle's cold
+    solutions z0, and the oracle's re-solves zr after an x0 disturbance U[-0.05, 0.05]^50 (tol
+    1e-4, Anderson memory 5).  Shared by the tests below: the oracle's solves take minutes."""
     from spock_gb300 import configs
     path, x0 = configs.cached("config2", tmp_problems, seed=0, count=32, cost_scale=1e-3)
     P = oracle_lib.Problem(path)
@@ -106,8 +104,19 @@ def test_fp32_bench_workload_against_fp64_oracle(oracle_lib, tmp_problems):
     assert (st == 0).all()
     x1 = np.clip(x0 + np.random.default_rng(3).uniform(-.05, .05, x0.shape), -1, 1)
     zr = z0.copy()
-    _, st, _, _, _ = P.solve_many_warm(x1, zr, opts, 16, warm=True)
+    _, st, its, _, _ = P.solve_many_warm(x1, zr, opts, 16, warm=True)
     assert (st == 0).all()
+    return path, P, x1, z0, zr, its
+
+
+def test_fp32_bench_workload_against_fp64_oracle(bench_resolves):
+    """The benchmark's step on its problem (config 2, costs x 1e-3): 32 instances at the FP64
+    oracle's cold solutions are re-solved after an x0 disturbance U[-0.05, 0.05]^50 to tol(1e-4),
+    by the FP32 batched solver on the GPU and by the FP64 oracle from the same starting point.
+    Both converge; the GPU's optimal costs s_0 are within 1e-2 (relative) and its first inputs u_0
+    within 1e-2 of the oracle's -- two stopping points of the same iteration at the same
+    tolerance, in FP32 and FP64 (the benchmark line reports the measured errors as fp64_error)."""
+    path, P, x1, z0, zr, _ = bench_resolves
     t, d, c = make(path, 32, batch=32, tol=1e-4, max_iters=20000, anderson=5)
     assert (c.runSpockBatch(x1, prev=z0) == 0).all()
     oS = P.size_prim - P.n
@@ -116,3 +125,29 @@ def test_fp32_bench_workload_against_fp64_oracle(oracle_lib, tmp_problems):
     ug, ur = zg[:, :P.nu] / P.scaling[P.nx:P.nx + P.nu], zr[:, :P.nu] / P.scaling[P.nx:P.nx + P.nu]
     print(f"FP32 vs FP64 at tol(1e-4): cost {cost_err.max():.3g} (max), u0 {np.abs(ug - ur).max():.3g} (max)")
     assert cost_err.max() <= 1e-2 and np.abs(ug - ur).max() <= 1e-2
+
+
+def test_fp64_finish_of_the_bench_workload(bench_resolves):
+    """The FP64 finish (spock_set_fp64_finish) on the benchmark's step: 64 instances (the 32
+    re-solves of the test above, each twice) start in FP32; after 20 rounds, once at most 32 are
+    running, those continue the same iteration in FP64 with their whole SuperMann state.  All
+    converge, both copies of an instance end identical (the move keeps slots apart), the
+    iteration counters run on across the move, and the optimal costs and first inputs agree with
+    the FP64 oracle's re-solves to 1e-2 as for the plain FP32 solve."""
+    path, P, x1, z0, zr, its_ref = bench_resolves
+    t, d, c = make(path, 32, batch=64, tol=1e-4, max_iters=20000, anderson=5)
+    c.fp64Finish(20)
+    assert (c.runSpockBatch(x1, prev=z0) == 0).all()
+    zg = c.solutions()
+    assert np.array_equal(zg[:32], zg[32:])
+    iters = c.countersAll()[:, 6]
+    assert np.array_equal(iters[:32], iters[32:]) and iters.max() > 20
+    oS = P.size_prim - P.n
+    zr2 = np.concatenate((zr, zr))
+    cost_err = np.abs(zg[:, oS] - zr2[:, oS]) / np.abs(zr2[:, oS])
+    scale_u = P.scaling[P.nx:P.nx + P.nu]
+    u_err = np.abs(zg[:, :P.nu] / scale_u - zr2[:, :P.nu] / scale_u).max()
+    print(f"FP32 + FP64 finish vs FP64 at tol(1e-4): cost {cost_err.max():.3g} (max), u0 {u_err:.3g} (max); "
+          f"outer iterations mean {iters.mean():.1f} max {iters.max()} (oracle mean {its_ref.mean():.1f} "
+          f"max {its_ref.max()})")
+    assert cost_err.max() <= 1e-2 and u_err <= 1e-2
