@@ -248,3 +248,91 @@ def test_python_factory_gpu_offline_at_config2_size(exe, tmp_path):
     assert abs(s_cpp - s_py) <= 1e-6 * s_py
     print(f"\nconfig-2 generation: python+numpy/ARPACK {t_host:.2f} s, python+GPU cache {t_gpu:.2f} s, "
           f"C++ generator+GPU cache {t_cpp:.2f} s")
+
+
+def _record_golden_inputs(case, monkeypatch, tmp_path):
+    """Run test_factory's builder of a golden case with the tree classes and the problem writer
+    intercepted: the raw inputs it passes (tree parameters, per-event dynamics and costs,
+    constraints, risk, preconditioning) become a spec for the C++ driver."""
+    import test_factory as TF
+    rec = {}
+
+    class Markov(F.MarkovChain):
+        def __init__(self, P, v, horizon, stopping_stage=None):
+            rec["tree"] = ("markov", np.asarray(P, float), np.asarray(v, float), horizon, stopping_stage)
+            super().__init__(P, v, horizon, stopping_stage)
+
+    class Iid(F.IidProcess):
+        def __init__(self, d, horizon, stopping_stage=None):
+            rec["tree"] = ("iid", np.asarray(d, float), horizon, stopping_stage)
+            super().__init__(d, horizon, stopping_stage)
+
+    def capture(self, path, dt="d", step_size=None, offline="host", device=0):
+        rec["factory"] = self
+
+    monkeypatch.setattr(F, "MarkovChain", Markov)
+    monkeypatch.setattr(F, "IidProcess", Iid)
+    monkeypatch.setattr(F.Factory, "generate_problem", capture)
+    TF.BUILDERS[case](str(tmp_path / "unused") + "/")
+    f, tr = rec["factory"], rec["tree"]
+    ne = len(f.dyn_events)
+    spec = dict(nx=f.nx, nu=f.nu, events=ne, dynamics="affine" if f.dyn_events[0].affine else "linear",
+                cost=f.cost_events[0].kind, leaf=f.leaf_cost.kind, nlcon=f.nl_con.kind, lcon=f.l_con.kind,
+                alpha=float(f.risk.alpha), precondition=int(bool(f.precondition)), scale=float(f.cost_scale), dtype="d")
+    if tr[0] == "markov":
+        spec.update(tree="markov", horizon=tr[3], stopping=tr[4] if tr[4] is not None else tr[3])
+        arr = dict(tree_P=tr[1], tree_v=tr[2])
+    else:
+        spec.update(tree="iid", horizon=tr[2], stopping=tr[3] if tr[3] is not None else tr[2])
+        arr = dict(tree_d=tr[1])
+    z = lambda shape: np.zeros(shape)
+    arr.update(dyn_A=np.array([d.A for d in f.dyn_events]), dyn_B=np.array([d.B for d in f.dyn_events]),
+               dyn_c=np.array([d.c for d in f.dyn_events])[:, :, None])
+    ce = f.cost_events
+    arr.update(cost_Q=np.array([c.Q if c.Q is not None else z((f.nx, f.nx)) for c in ce]),
+               cost_R=np.array([c.R if c.R is not None else z((f.nu, f.nu)) for c in ce]),
+               cost_q=np.array([c.q if c.q is not None else z(f.nx) for c in ce])[:, :, None],
+               cost_r=np.array([c.r if c.r is not None else z(f.nu) for c in ce])[:, :, None],
+               leaf_Q=(f.leaf_cost.Q if f.leaf_cost.Q is not None else z((f.nx, f.nx)))[None],
+               leaf_q=f.leaf_cost.q if f.leaf_cost.q is not None else z(f.nx))
+    for p, con in (("nl_", f.nl_con), ("l_", f.l_con)):
+        if con.kind in ("rectangle", "polyhedronWithIdentity", "rectangleInputBall"):
+            n_id = con.nx if con.kind == "rectangleInputBall" else con.lb.size
+            arr.update({p + "lb": con.lb[:n_id], p + "ub": con.ub[:n_id]})
+        if con.kind in ("polyhedron", "polyhedronWithIdentity"):
+            arr.update({p + "G": con.G, p + "glb": con.glb if con.kind == "polyhedronWithIdentity" else con.lb,
+                        p + "gub": con.gub if con.kind == "polyhedronWithIdentity" else con.ub})
+        if con.kind == "rectangleInputBall":
+            spec["radius"] = con.radius
+    return spec, arr
+
+
+@pytest.mark.parametrize("case", ["reftest", "cfg1", "qpl", "affpoly"])
+def test_cpp_problem_data_matches_reference_golden(exe, tmp_path, monkeypatch, case):
+    """The C++ generator on the raw inputs of a golden case against the folder the reference's
+    own Python factory wrote (tests/golden/<case>): every problem-data tensor (the offline cache
+    aside) and every data.json key but the step size."""
+    from conftest import GOLDEN
+    spec, arr = _record_golden_inputs(case, monkeypatch, tmp_path)
+    write_inputs(str(tmp_path / "in"), spec, arr)
+    r = subprocess.run([exe, "data", str(tmp_path / "in"), str(tmp_path / "cpp")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    ref_dir, mine = os.path.join(GOLDEN, case), str(tmp_path / "cpp")
+    ref_files = sorted(f for f in os.listdir(ref_dir) if f.endswith(".bt") and not f.startswith(("test_", "initialState"))
+                       and f.rsplit("_", 1)[0] not in CACHE)
+    assert sorted(f for f in os.listdir(mine) if f.endswith(".bt")) == ref_files
+    for f in ref_files:
+        (a, da), (b, db) = read_bt(os.path.join(ref_dir, f)), read_bt(os.path.join(mine, f))
+        assert da == db, f
+        if f.endswith("_u.bt"):
+            assert np.array_equal(a, b), f
+            continue
+        # the reference's sqrtm of the root's all-zero cost matrix (never read) is not finite
+        fin = np.isfinite(a)
+        scale = max(1., np.abs(a[fin]).max()) if fin.any() else 1.
+        assert np.abs(a[fin] - b[fin]).max(initial=0.) <= 1e-10 * scale, f
+    ref_meta = json.load(open(os.path.join(ref_dir, "data.json")))
+    meta = json.load(open(os.path.join(mine, "data.json")))
+    for k, v in ref_meta.items():
+        if k not in ("stepSize", "rowsS2"):
+            assert meta[k] == v, k
