@@ -1704,10 +1704,17 @@ private:
             CK(cudaGetLastError());
             return;
         }
-        const long bx = (gB() + 255) / 256;  // about 8 blocks of 256 threads per SM
-        const long by = std::max<long>(1, std::min<long>((152 * 8 + bx - 1) / bx, D_.sZ));
+        // Blocks as wide as the slots the round covers, at most 256 (k_update takes its instance
+        // from blockIdx.x * blockDim.x + threadIdx.x and its rows from blockIdx.y): after a
+        // compaction to one tile, 256-wide blocks would leave 7 of 8 threads without an instance.
+        // As many threads as about 8 blocks of 256 per SM.
+        const long live = gB();
+        const int tx = live >= 256 ? 256 : (int)((live + 31) / 32 * 32);
+        const long bx = (live + tx - 1) / tx;
+        const long blocks = 152L * 8 * 256 / tx;
+        const long by = std::max<long>(1, std::min<long>((blocks + bx - 1) / bx, D_.sZ));
         withAnderson([&](auto mc) {
-            k_update<T, decltype(mc)::value><<<dim3((unsigned)bx, (unsigned)by), 256, 0, stream_>>>(D_, A);
+            k_update<T, decltype(mc)::value><<<dim3((unsigned)bx, (unsigned)by), tx, 0, stream_>>>(D_, A);
         });
         CK(cudaGetLastError());
     }
