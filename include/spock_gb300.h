@@ -188,8 +188,10 @@ int spock_set_tuning(spock_solver s, const int *in3);
  * whole SuperMann state (iterate, Anderson memory, controller state, tolerance) into an FP64
  * solver of the same problem, made on first use with batch 32, which continues the same
  * iteration in FP64 until they stop; their final iterates, statuses and counters come back.
- * rounds = 0 (the default) turns it off.  No effect on FP64 solvers or batches below 32.  No
- * reference counterpart: the reference iterates in one precision (cache.cuh:1008-1132). */
+ * rounds = 0 (the default) turns it off.  No effect on FP64 solvers or batches below 32; where
+ * the problem has no FP64 batched kernels (node data beyond their shared memory) the solve
+ * continues in FP32 and the finish turns itself off.  No reference counterpart: the reference
+ * iterates in one precision (cache.cuh:1008-1132). */
 int spock_set_fp64_finish(spock_solver s, long rounds);
 
 /* Dynamics projection that allocates no device memory.  No counterpart in the reference: it

@@ -771,10 +771,11 @@ public:
                     if (maybeCompact(act)) round = graphFor(levelFor(capacity_));
                     if (finishAfter_ > 0 && rounds >= finishAfter_ && act <= kTileB && sizeof(T) == 4 && batched_) {
                         long r2 = 0, l2 = 0;
-                        finishInDouble(t0, r2, l2);
-                        rounds += (int)r2;
-                        launches += l2;
-                        break;
+                        if (finishInDouble(t0, r2, l2)) {
+                            rounds += (int)r2;
+                            launches += l2;
+                            break;
+                        }
                     }
                 }
             }
@@ -1865,7 +1866,9 @@ private:
     // stop; their final iterates and controller state (status, counters) come back converted.
     // Only the arithmetic of the remaining iterations changes: an FP32 instance that stalls near
     // the tolerance on float rounding finishes in the FP64 number of iterations.
-    void finishInDouble(std::chrono::steady_clock::time_point t0, long &rounds, long &launches) {
+    // Returns false, and turns the finish off, when this problem has no FP64 batched kernels (its
+    // node data exceed their shared memory): the solve then continues in FP32.
+    bool finishInDouble(std::chrono::steady_clock::time_point t0, long &rounds, long &launches) {
         if constexpr (sizeof(T) == 4) {
             std::vector<int> st((size_t)B_);
             CK(cudaMemcpyAsync(st.data(), S_.status, sizeof(int) * (size_t)B_, cudaMemcpyDeviceToHost, stream_));
@@ -1874,9 +1877,14 @@ private:
             for (long q = 0; q < B_ && (long)idx.size() < kTileB; q++)
                 if (st[(size_t)q] == -1) idx.push_back((int)q);
             const int count = (int)idx.size();
-            if (count == 0) return;
+            if (count == 0) return false;
             if (!twin_) {  // made, tuned and captured before any state moves in
-                twin_.reset(new Engine<double>(hp_, opt_, kTileB, device_));
+                try {
+                    twin_.reset(new Engine<double>(hp_, opt_, kTileB, device_));
+                } catch (const std::invalid_argument &) {
+                    finishAfter_ = 0;
+                    return false;
+                }
                 twinIdx_ = dalloc<int>(2 * kTileB);
                 twin_->ensureGraph();
                 CK(cudaStreamSynchronize(twin_->stream_));
@@ -1923,7 +1931,9 @@ private:
             CK(cudaGetLastError());
             CK(cudaStreamSynchronize(stream_));
             launches += 2 * (7 + 2 * opt_.anderson) + 4;
+            return true;
         }
+        return false;
     }
 
     // Run rounds on the state already in place (no re-initialisation) until every instance stops.
