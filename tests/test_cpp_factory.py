@@ -336,3 +336,17 @@ def test_cpp_problem_data_matches_reference_golden(exe, tmp_path, monkeypatch, c
     for k, v in ref_meta.items():
         if k not in ("stepSize", "rowsS2"):
             assert meta[k] == v, k
+
+
+def test_gpu_offline_cache_fails_loudly_without_a_gpu(tmp_path):
+    """The offline cache is GPU code with no host fallback: without a device the Python factory's
+    offline="gpu" path raises, after writing the problem data."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    sg.build()
+    spec, arr = make_case("cfg1")
+    with pytest.raises(RuntimeError):
+        python_factory(spec, arr, str(tmp_path / "p") + "/", offline="gpu")
+    assert os.path.exists(tmp_path / "p" / "dynamics_AB_d.bt")
+    assert not os.path.exists(tmp_path / "p" / "dynamics_P_d.bt")
