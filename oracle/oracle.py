@@ -86,6 +86,7 @@ def lib():
 # FP32 emulation modes (spock_oracle.h): problem data, matvec accumulation, vector storage,
 # Anderson normal equations, and the two remedies for the forward rollout.
 EMU_DATA, EMU_ACC, EMU_VEC, EMU_GRAM, EMU_FWD64, EMU_FWDC, EMU_FWDCX, EMU_FWDK = 1, 2, 4, 8, 16, 32, 64, 128
+EMU_ACCX_OPS, EMU_ACCX_BACK = 256, 512  # exact accumulation in L / L*, or in the backward sweep
 EMU_GPU_FP32 = EMU_DATA | EMU_ACC | EMU_VEC | EMU_GRAM
 
 

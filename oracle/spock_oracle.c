@@ -64,6 +64,9 @@ static char g_err[2048];
 /* FP32 emulation mode (spock_oracle.h, OR_EMU_*); 0 keeps every operation in double. */
 static int g_emu = 0;
 void or_set_emulation(int mode) { g_emu = mode; }
+/* Nonzero while a region whose products OR_EMU_ACCX_* exempts from OR_EMU_ACC runs (per thread:
+ * the batch solves run one instance per thread). */
+static __thread int g_exact = 0;
 static void r32(double *v, long n) {
     for (long i = 0; i < n; i++) v[i] = (double)(float)v[i];
 }
@@ -413,7 +416,7 @@ void or_scaling(const OrProblem *p, double *out) { memcpy(out, p->scaling, sizeo
 
 /* y (+)= M x, M column-major r x c */
 static inline void matvec(const double *M, long r, long c, const double *x, double *y, int add) {
-    if (g_emu & OR_EMU_ACC) {
+    if ((g_emu & OR_EMU_ACC) && !g_exact) {
         for (long i = 0; i < r; i++) {
             float acc = add ? (float)y[i] : 0.f;
             for (long k = 0; k < c; k++) acc = fmaf((float)M[k * r + i], (float)x[k], acc);
@@ -431,7 +434,7 @@ static inline void matvec(const double *M, long r, long c, const double *x, doub
 
 /* y (+)= M' x, M column-major r x c, x length r, y length c */
 static inline void matTvec(const double *M, long r, long c, const double *x, double *y, int add) {
-    if (g_emu & OR_EMU_ACC) {
+    if ((g_emu & OR_EMU_ACC) && !g_exact) {
         for (long k = 0; k < c; k++) {
             float acc = 0.f;
             for (long i = 0; i < r; i++) acc = fmaf((float)M[k * r + i], (float)x[i], acc);
@@ -497,7 +500,24 @@ static inline double dotv(const double *a, const double *b, long n) {
 
 /* ------------------------------------------------------------------ L and L* */
 
+static void op_impl(const OrProblem *p, const double *prim, double *dual);
+static void adj_impl(const OrProblem *p, const double *dual, double *prim);
+
 void or_op(const OrProblem *p, const double *prim, double *dual) {
+    const int saved = g_exact;
+    if (g_emu & OR_EMU_ACCX_OPS) g_exact = 1;
+    op_impl(p, prim, dual);
+    g_exact = saved;
+}
+
+void or_adj(const OrProblem *p, const double *dual, double *prim) {
+    const int saved = g_exact;
+    if (g_emu & OR_EMU_ACCX_OPS) g_exact = 1;
+    adj_impl(p, dual, prim);
+    g_exact = saved;
+}
+
+static void op_impl(const OrProblem *p, const double *prim, double *dual) {
     const long nx = p->nx, nu = p->nu, nxu = p->nxu, yD = p->yDim, n = p->n, nnl = p->nnl;
     const double *u = prim, *x = prim + p->oX, *y = prim + p->oY, *t = prim + p->oT, *s = prim + p->oS;
     double *I = dual, *II = dual + p->oII, *III = dual + p->oIII, *IV = dual + p->oIV, *V = dual + p->oV,
@@ -563,7 +583,7 @@ void or_op(const OrProblem *p, const double *prim, double *dual) {
     EMU_VEC(dual, p->sDual);
 }
 
-void or_adj(const OrProblem *p, const double *dual, double *prim) {
+static void adj_impl(const OrProblem *p, const double *dual, double *prim) {
     const long nx = p->nx, nu = p->nu, nxu = p->nxu, yD = p->yDim, n = p->n, nnl = p->nnl;
     double *u = prim, *x = prim + p->oX, *y = prim + p->oY, *t = prim + p->oT, *s = prim + p->oS;
     const double *I = dual, *II = dual + p->oII, *III = dual + p->oIII, *IV = dual + p->oIV, *V = dual + p->oV,
@@ -651,6 +671,8 @@ void or_project_dynamics(const OrProblem *p, const double *x0, double *x, double
     double tmp[1024];
     for (long j = nnl; j < n; j++)
         for (long k = 0; k < nx; k++) q[j * nx + k] = -x[j * nx + k];
+    const int saved = g_exact;
+    if (g_emu & OR_EMU_ACCX_BACK) g_exact = 1;
     for (long stage = p->ns - 2; stage >= 0; stage--) {
         for (long i = p->stageFrom[stage]; i <= p->stageTo[stage]; i++) {
             const long c0 = p->chFrom[i], nc = p->numCh[i];
@@ -679,6 +701,7 @@ void or_project_dynamics(const OrProblem *p, const double *x0, double *x, double
             }
         }
     }
+    g_exact = saved;
     for (long k = 0; k < nx; k++) x[k] = x0[k];
     EMU_VEC(x, nx);
     for (long stage = 0; stage < p->ns - 1; stage++) {

@@ -102,9 +102,12 @@ double or_norm_L_sq(const OrProblem *p, long iters);
  *                 algorithm: error-free products by FMA, TwoSum additions);
  *   OR_EMU_FWDCX  the same for the children's states [A B][x; u] only (u = Kx + d plain);
  *   OR_EMU_FWDK   the forward rollout with Kahan's compensated summation of the rounded float
- *                 products (half the operations of Dot2; the products' own errors remain). */
+ *                 products (half the operations of Dot2; the products' own errors remain);
+ *   OR_EMU_ACCX_OPS   L and L* accumulate exactly although OR_EMU_ACC is set;
+ *   OR_EMU_ACCX_BACK  the dynamics projection's backward sweep accumulates exactly although
+ *                     OR_EMU_ACC is set. */
 enum { OR_EMU_DATA = 1, OR_EMU_ACC = 2, OR_EMU_VEC = 4, OR_EMU_GRAM = 8, OR_EMU_FWD64 = 16, OR_EMU_FWDC = 32,
-       OR_EMU_FWDCX = 64, OR_EMU_FWDK = 128 };
+       OR_EMU_FWDCX = 64, OR_EMU_FWDK = 128, OR_EMU_ACCX_OPS = 256, OR_EMU_ACCX_BACK = 512 };
 void or_set_emulation(int mode);
 
 #ifdef __cplusplus
