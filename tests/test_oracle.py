@@ -241,3 +241,30 @@ def test_fp32_emulation_forward_rollout(oracle_lib, tmp_problems):
         oracle_lib.set_emulation(0)
     assert err["vec"] < err["dot2"] < err["acc"] and err["fwd64"] < err["acc"]
     assert err["acc"] < 1e-5 and err["dot2"] < 0.6 * err["acc"]
+
+
+def test_fp32_emulation_backward_sweep(oracle_lib, tmp_problems):
+    """With the forward rollout compensated (Dot2, as on the GPU), the rest of the dynamics
+    projection's deviation from FP64 on a config-2 sized problem comes from the backward sweep's
+    float accumulation: accumulating that sweep exactly (OR_EMU_ACCX_BACK) halves it, while the
+    scope of L and L* (OR_EMU_ACCX_OPS) does not touch the projection."""
+    from spock_gb300 import configs
+    path, x0 = configs.cached("config2", tmp_problems, seed=0, count=1, cost_scale=1e-3)
+    rng = np.random.default_rng(0)
+    P0 = oracle_lib.Problem(path)
+    x = rng.standard_normal(P0.nx * P0.n)
+    u = rng.standard_normal(P0.nu * P0.nnl)
+    x0s = (x0[0] * P0.scaling[:P0.nx]).astype(np.float32).astype(np.float64)
+    gpu = oracle_lib.EMU_DATA | oracle_lib.EMU_ACC | oracle_lib.EMU_VEC | oracle_lib.EMU_FWDC
+    err = {}
+    try:
+        oracle_lib.set_emulation(oracle_lib.EMU_DATA)
+        ref = np.concatenate(oracle_lib.Problem(path).project_dynamics(x0s, x, u))
+        for name, mode in [("dot2", gpu), ("back", gpu | oracle_lib.EMU_ACCX_BACK),
+                           ("ops", gpu | oracle_lib.EMU_ACCX_OPS)]:
+            oracle_lib.set_emulation(mode)
+            out = np.concatenate(oracle_lib.Problem(path).project_dynamics(x0s, x, u))
+            err[name] = np.abs(out - ref).max() / np.abs(ref).max()
+    finally:
+        oracle_lib.set_emulation(0)
+    assert err["back"] < 0.6 * err["dot2"] and err["ops"] == err["dot2"], err
